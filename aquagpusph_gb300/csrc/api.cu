@@ -1,0 +1,672 @@
+// C ABI of the aqua_gb300 library: context, device memory, step scheduling
+// (CUDA graphs) and the reference-facing entry points.
+//
+// Ownership mirrors the reference's CalcServer (CalcServer.cpp:139-535,
+// 566-569): the context owns every device buffer of the resident case (two
+// sets of particle Variables that alternate between steps, plus the step
+// scratch) and allocates them all at creation; steps allocate nothing.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "aqua_internal.cuh"
+#include "kernels.cuh"
+
+using namespace aqua;
+
+struct aqua_ctx
+{
+    int device = 0;
+    int dims = 3;
+    uint32_t capacity = 0;  // max particles
+    uint32_t ncap = 0;      // cell capacity
+    uint32_t N = 0;
+    uint32_t passes = 3;
+    Consts consts{};
+    VarSet set[2]{};
+    int cur = 0;
+    StepBufs b{};
+    DevScalars* sc = nullptr;      // resident state scalars
+    DevScalars* sc_aux = nullptr;  // standalone link-list / sort
+    uint32_t* ihoc_out = nullptr;  // ihoc export buffer (ncap)
+    int extras = 0;
+    void* pool = nullptr;
+    size_t pool_bytes = 0;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t graph[2] = { nullptr, nullptr };
+    // stage boundary events (recorded when profiling is on): before the
+    // link-list, before the gather, before the sweep, after the sweep, end
+    static constexpr int kEvents = 5;
+    cudaEvent_t ev[kEvents] = {};
+    int profiling = 0;
+};
+
+namespace {
+
+#define AQ_CUDA(call)                                                          \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            std::fprintf(stderr, "aqua_gb300: %s failed: %s\n", #call,         \
+                         cudaGetErrorString(e_));                              \
+            return AQUA_ERR_CUDA;                                              \
+        }                                                                      \
+    } while (0)
+
+struct Carver
+{
+    char* base;
+    size_t off = 0;
+    template<typename T>
+    T* take(size_t count)
+    {
+        off = (off + 255) & ~(size_t)255;
+        T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+aqua_status
+build_consts(const aqua_params* p, Consts& c)
+{
+    if (!p || (p->dims != 2 && p->dims != 3) || p->n_sets == 0 ||
+        p->n_sets > (uint32_t)kMaxSets || !p->refd || !p->visc_dyn ||
+        !p->delta || !(p->h > 0.f) || !(p->support > 0.f) || !(p->H > 0.f))
+        return AQUA_ERR_INVALID;
+    if (p->iter_midpoint_max != 1)
+        return AQUA_ERR_INVALID;  // one midpoint iteration (canonical stack)
+    std::memset(&c, 0, sizeof(c));
+    c.dims = p->dims;
+    c.n_sets = p->n_sets;
+    c.h = p->h;
+    c.support = p->support;
+    c.H = p->H;
+    c.CONW = p->CONW;
+    c.CONF = p->CONF;
+    c.SUPPORT = p->SUPPORT;
+    c.DIMS = p->DIMS;
+    c.cs = p->cs;
+    c.p0 = p->p0;
+    std::memcpy(c.g, p->g, sizeof(c.g));
+    c.courant = p->courant;
+    c.dt_Ma = p->dt_Ma;
+    c.dt_min = p->dt_min;
+    c.dt_fixed = p->dt_fixed;
+    std::memcpy(c.domain_min, p->domain_min, sizeof(c.domain_min));
+    std::memcpy(c.domain_max, p->domain_max, sizeof(c.domain_max));
+    c.dr_factor = p->dr_factor;
+    c.min_bound_dist = p->min_bound_dist;
+    c.relax_midpoint = p->relax_midpoint;
+    c.iter_midpoint_max = p->iter_midpoint_max;
+    for (uint32_t k = 0; k < p->n_sets; k++) {
+        c.refd[k] = p->refd[k];
+        c.visc_dyn[k] = p->visc_dyn[k];
+        c.delta[k] = p->delta[k];
+    }
+    // LinkList.cpp:156 and LinkList.cl.in:73, both in float
+    volatile float sh = p->support * p->h;
+    c.cell_length = sh;
+    c.idist = 1.f / sh;
+    // |r_ij|^2 at or above this bound gives |r_ij| / H >= SUPPORT for sure;
+    // pairs below it take the exact test
+    const double lim = (double)p->SUPPORT * (double)p->H;
+    c.q2_reject = (float)(lim * lim * (1.0 + 1.0e-4));
+    return AQUA_OK;
+}
+
+uint32_t
+cells_from_domain(const aqua_params* p)
+{
+    const float cl = p->support * p->h;
+    unsigned long long n = 1;
+    for (int k = 0; k < p->dims; k++) {
+        const double span = (double)p->domain_max[k] - (double)p->domain_min[k];
+        if (!(span > 0))
+            return 0;
+        n *= (unsigned long long)(span / cl) + 8ull;
+    }
+    return n > 0xffffffffull ? 0u : (uint32_t)n;
+}
+
+uint32_t
+bits_for(uint32_t maxval)
+{
+    uint32_t b = 0;
+    while (b < 32 && (1ull << b) <= maxval)
+        b++;
+    return b;
+}
+
+size_t
+layout(aqua_ctx* x, char* base)
+{
+    Carver cv{ base };
+    const uint32_t n = x->capacity;
+    const int VS = (x->dims == 3) ? 4 : 2;
+    for (int s = 0; s < 2; s++) {
+        VarSet& v = x->set[s];
+        v.id = cv.take<uint32_t>(n);
+        v.iset = cv.take<uint32_t>(n);
+        v.imove = cv.take<int32_t>(n);
+        v.r = cv.take<float>((size_t)n * VS);
+        v.normal = cv.take<float>((size_t)n * VS);
+        v.tangent = cv.take<float>((size_t)n * VS);
+        v.binormal = cv.take<float>((size_t)n * VS);
+        v.u = cv.take<float>((size_t)n * VS);
+        v.dudt = cv.take<float>((size_t)n * VS);
+        v.rho = cv.take<float>(n);
+        v.drhodt = cv.take<float>(n);
+        v.m = cv.take<float>(n);
+        v.p = cv.take<float>(n);
+    }
+    StepBufs& b = x->b;
+    const uint32_t nb = sort_blocks(n > 0 ? n : 1);
+    for (int k = 0; k < 2; k++) {
+        b.keys[k] = cv.take<uint32_t>(n);
+        b.vals[k] = cv.take<uint32_t>(n);
+    }
+    b.counts = cv.take<uint32_t>((size_t)256 * nb);
+    b.digit_total = cv.take<uint32_t>(256);
+    b.cells = cv.take<uint2>(x->ncap);
+    b.cell_wall = cv.take<uint8_t>(x->ncap);
+    b.id_sorted = cv.take<uint32_t>(n);
+    b.r_in = cv.take<float>((size_t)n * VS);
+    b.u_in = cv.take<float>((size_t)n * VS);
+    b.dudt_in = cv.take<float>((size_t)n * VS);
+    b.rho_in = cv.take<float>(n);
+    b.drhodt_in = cv.take<float>(n);
+    b.posq = cv.take<float4>(n);
+    b.velq = cv.take<float4>(n);
+    b.pmq = cv.take<float2>(n);
+    b.grad_p = cv.take<float>((size_t)n * VS);
+    b.lap_u = cv.take<float>((size_t)n * VS);
+    b.div_u = cv.take<float>(n);
+    b.lap_p = cv.take<float>(n);
+    b.grad_w_bi = cv.take<float>((size_t)n * VS);
+    b.div_u_bi = cv.take<float>(n);
+    b.shepard = cv.take<float>(n);
+    x->sc = cv.take<DevScalars>(1);
+    x->sc_aux = cv.take<DevScalars>(1);
+    x->ihoc_out = cv.take<uint32_t>(x->ncap);
+    return cv.off + 256;
+}
+
+void
+drop_graphs(aqua_ctx* x)
+{
+    for (int k = 0; k < 2; k++) {
+        if (x->graph[k])
+            cudaGraphExecDestroy(x->graph[k]);
+        x->graph[k] = nullptr;
+    }
+}
+
+// Launches one step on `s` (the resident state advances from set[cur] to
+// set[cur ^ 1]; the caller flips cur).
+aqua_status
+enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
+{
+    const VarSet& S = x->set[cur];
+    const VarSet& T = x->set[cur ^ 1];
+    StepBufs& b = x->b;
+    const uint32_t N = x->N;
+    if (x->profiling)
+        AQ_CUDA(cudaEventRecord(x->ev[0], s));
+    AQ_CUDA(launch_begin(x->sc, b.cells, b.cell_wall, x->ncap, N, s));
+    if (x->dims == 3) {
+        AQ_CUDA(launch_minmax<3>(x->consts, S.r, S.imove, N, x->sc, s));
+        AQ_CUDA(launch_icell_hist<3>(x->consts, S.r, S.imove, N, x->sc, x->ncap,
+                                     b.keys[0], b.vals[0], b.counts, s));
+    } else {
+        AQ_CUDA(launch_minmax<2>(x->consts, S.r, S.imove, N, x->sc, s));
+        AQ_CUDA(launch_icell_hist<2>(x->consts, S.r, S.imove, N, x->sc, x->ncap,
+                                     b.keys[0], b.vals[0], b.counts, s));
+    }
+    AQ_CUDA(launch_radix_passes(b.keys, b.vals, N, x->passes, b.counts,
+                                b.digit_total, true, x->sc, s));
+    StepArgs a;
+    a.N = N;
+    a.ncap = x->ncap;
+    a.src = S;
+    a.dst = T;
+    a.b = b;
+    a.skeys = b.keys[x->passes & 1];
+    a.perm = b.vals[x->passes & 1];
+    a.sc = x->sc;
+    a.extras = x->extras;
+    if (x->profiling)
+        AQ_CUDA(cudaEventRecord(x->ev[1], s));
+    if (x->dims == 3)
+        AQ_CUDA(launch_gather<3>(x->consts, a, s));
+    else
+        AQ_CUDA(launch_gather<2>(x->consts, a, s));
+    if (x->profiling)
+        AQ_CUDA(cudaEventRecord(x->ev[2], s));
+    if (x->dims == 3)
+        AQ_CUDA(launch_sweep<3>(x->consts, a, s));
+    else
+        AQ_CUDA(launch_sweep<2>(x->consts, a, s));
+    if (x->profiling)
+        AQ_CUDA(cudaEventRecord(x->ev[3], s));
+    AQ_CUDA(launch_finalize(x->sc, s));
+    if (x->profiling)
+        AQ_CUDA(cudaEventRecord(x->ev[4], s));
+    return AQUA_OK;
+}
+
+aqua_status
+copy_in(void* dst, const void* src, size_t bytes, int on_host, cudaStream_t s)
+{
+    if (!src)
+        return AQUA_ERR_INVALID;
+    AQ_CUDA(cudaMemcpyAsync(dst, src, bytes,
+                            on_host ? cudaMemcpyHostToDevice
+                                    : cudaMemcpyDeviceToDevice, s));
+    return AQUA_OK;
+}
+
+aqua_status
+copy_out(void* dst, const void* src, size_t bytes, int on_host, cudaStream_t s)
+{
+    if (!dst)
+        return AQUA_OK;
+    AQ_CUDA(cudaMemcpyAsync(dst, src, bytes,
+                            on_host ? cudaMemcpyDeviceToHost
+                                    : cudaMemcpyDeviceToDevice, s));
+    return AQUA_OK;
+}
+
+#define AQ_TRY(expr)                                                           \
+    do {                                                                       \
+        aqua_status st_ = (expr);                                              \
+        if (st_ != AQUA_OK)                                                    \
+            return st_;                                                        \
+    } while (0)
+
+aqua_status
+status_of(uint32_t err)
+{
+    if (err & kErrCapacity)
+        return AQUA_ERR_CAPACITY;
+    if (err & kErrNonFinite)
+        return AQUA_ERR_NONFINITE;
+    if (err & kErrDt)
+        return AQUA_ERR_DT;
+    return AQUA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char*
+aqua_version(void)
+{
+    return "aqua_gb300 0.1 (sm_103a)";
+}
+
+aqua_status
+aqua_create(const aqua_params* params, uint32_t capacity,
+            uint32_t ihoc_capacity, aqua_ctx** out)
+{
+    if (!out || capacity == 0)
+        return AQUA_ERR_INVALID;
+    *out = nullptr;
+    Consts c;
+    AQ_TRY(build_consts(params, c));
+    aqua_ctx* x = new (std::nothrow) aqua_ctx();
+    if (!x)
+        return AQUA_ERR_NO_MEMORY;
+    x->consts = c;
+    x->dims = params->dims;
+    x->capacity = capacity;
+    x->ncap = ihoc_capacity ? ihoc_capacity : cells_from_domain(params);
+    if (x->ncap == 0) {
+        delete x;
+        return AQUA_ERR_INVALID;
+    }
+    x->passes = sort_passes(bits_for(x->ncap));
+    if (cudaGetDevice(&x->device) != cudaSuccess) {
+        delete x;
+        return AQUA_ERR_CUDA;
+    }
+    x->pool_bytes = layout(x, nullptr);
+    if (cudaMalloc(&x->pool, x->pool_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        delete x;
+        return AQUA_ERR_NO_MEMORY;
+    }
+    layout(x, (char*)x->pool);
+    for (int k = 0; k < aqua_ctx::kEvents; k++)
+        if (cudaEventCreate(&x->ev[k]) != cudaSuccess) {
+            cudaFree(x->pool);
+            delete x;
+            return AQUA_ERR_CUDA;
+        }
+    if (cudaMemset(x->pool, 0, x->pool_bytes) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&x->cap_stream, cudaStreamNonBlocking) !=
+            cudaSuccess) {
+        cudaFree(x->pool);
+        delete x;
+        return AQUA_ERR_CUDA;
+    }
+    *out = x;
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_destroy(aqua_ctx* x)
+{
+    if (!x)
+        return AQUA_ERR_INVALID;
+    drop_graphs(x);
+    if (x->cap_stream)
+        cudaStreamDestroy(x->cap_stream);
+    for (int k = 0; k < aqua_ctx::kEvents; k++)
+        if (x->ev[k])
+            cudaEventDestroy(x->ev[k]);
+    if (x->pool)
+        cudaFree(x->pool);
+    delete x;
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_set_params(aqua_ctx* x, const aqua_params* params)
+{
+    if (!x || !params || params->dims != x->dims)
+        return AQUA_ERR_INVALID;
+    Consts c;
+    AQ_TRY(build_consts(params, c));
+    x->consts = c;
+    drop_graphs(x);
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_set_extras(aqua_ctx* x, int on)
+{
+    if (!x)
+        return AQUA_ERR_INVALID;
+    x->extras = on ? 1 : 0;
+    drop_graphs(x);
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_set_state(aqua_ctx* x, uint32_t N, const aqua_vars* v, int on_host,
+               float t, float dt, uint32_t iter, void* stream)
+{
+    if (!x || !v || N == 0 || N > x->capacity)
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t VS = (x->dims == 3) ? 4 : 2;
+    VarSet& d = x->set[x->cur];
+    AQ_TRY(copy_in(d.id, v->id, N * 4ull, on_host, s));
+    AQ_TRY(copy_in(d.iset, v->iset, N * 4ull, on_host, s));
+    AQ_TRY(copy_in(d.imove, v->imove, N * 4ull, on_host, s));
+    AQ_TRY(copy_in(d.r, v->r, N * VS * 4, on_host, s));
+    AQ_TRY(copy_in(d.normal, v->normal, N * VS * 4, on_host, s));
+    AQ_TRY(copy_in(d.tangent, v->tangent, N * VS * 4, on_host, s));
+    if (v->binormal)
+        AQ_TRY(copy_in(d.binormal, v->binormal, N * VS * 4, on_host, s));
+    AQ_TRY(copy_in(d.u, v->u, N * VS * 4, on_host, s));
+    AQ_TRY(copy_in(d.dudt, v->dudt, N * VS * 4, on_host, s));
+    AQ_TRY(copy_in(d.rho, v->rho, N * 4ull, on_host, s));
+    AQ_TRY(copy_in(d.drhodt, v->drhodt, N * 4ull, on_host, s));
+    AQ_TRY(copy_in(d.m, v->m, N * 4ull, on_host, s));
+    AQ_TRY(copy_in(d.p, v->p, N * 4ull, on_host, s));
+    if (N != x->N)
+        drop_graphs(x);
+    x->N = N;
+    DevScalars hs;
+    std::memset(&hs, 0, sizeof(hs));
+    hs.t = t;
+    hs.dt = dt;
+    hs.iter = iter;
+    hs.dt_next = 0x7f800000u;
+    // pageable source: the copy completes before the call returns
+    AQ_CUDA(cudaMemcpyAsync(x->sc, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(cudaStreamSynchronize(s));
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_get_state(aqua_ctx* x, aqua_vars* v, int on_host, void* stream)
+{
+    if (!x || !v || x->N == 0)
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t N = x->N, VS = (x->dims == 3) ? 4 : 2;
+    const VarSet& d = x->set[x->cur];
+    AQ_TRY(copy_out(v->id, d.id, N * 4, on_host, s));
+    AQ_TRY(copy_out(v->iset, d.iset, N * 4, on_host, s));
+    AQ_TRY(copy_out(v->imove, d.imove, N * 4, on_host, s));
+    AQ_TRY(copy_out(v->r, d.r, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(v->normal, d.normal, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(v->tangent, d.tangent, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(v->binormal, d.binormal, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(v->u, d.u, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(v->dudt, d.dudt, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(v->rho, d.rho, N * 4, on_host, s));
+    AQ_TRY(copy_out(v->drhodt, d.drhodt, N * 4, on_host, s));
+    AQ_TRY(copy_out(v->m, d.m, N * 4, on_host, s));
+    AQ_TRY(copy_out(v->p, d.p, N * 4, on_host, s));
+    AQ_TRY(copy_out(v->shepard, x->b.shepard, N * 4, on_host, s));
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_get_extra(aqua_ctx* x, aqua_extra* e, int on_host, void* stream)
+{
+    if (!x || !e || x->N == 0)
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t N = x->N, VS = (x->dims == 3) ? 4 : 2;
+    const StepBufs& b = x->b;
+    AQ_TRY(copy_out(e->r_in, b.r_in, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(e->u_in, b.u_in, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(e->dudt_in, b.dudt_in, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(e->rho_in, b.rho_in, N * 4, on_host, s));
+    AQ_TRY(copy_out(e->drhodt_in, b.drhodt_in, N * 4, on_host, s));
+    AQ_TRY(copy_out(e->icell, b.keys[x->passes & 1], N * 4, on_host, s));
+    AQ_TRY(copy_out(e->id_unsorted, b.vals[x->passes & 1], N * 4, on_host, s));
+    AQ_TRY(copy_out(e->id_sorted, b.id_sorted, N * 4, on_host, s));
+    if (e->ihoc) {
+        if (x->dims == 3)
+            AQ_CUDA(launch_export_ihoc<3>(b.cells, x->ihoc_out, x->ncap, x->sc, s));
+        else
+            AQ_CUDA(launch_export_ihoc<2>(b.cells, x->ihoc_out, x->ncap, x->sc, s));
+        AQ_TRY(copy_out(e->ihoc, x->ihoc_out, (size_t)x->ncap * 4, on_host, s));
+    }
+    AQ_TRY(copy_out(e->grad_p, b.grad_p, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(e->lap_u, b.lap_u, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(e->div_u, b.div_u, N * 4, on_host, s));
+    AQ_TRY(copy_out(e->lap_p, b.lap_p, N * 4, on_host, s));
+    AQ_TRY(copy_out(e->grad_w_bi, b.grad_w_bi, N * VS * 4, on_host, s));
+    AQ_TRY(copy_out(e->div_u_bi, b.div_u_bi, N * 4, on_host, s));
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_get_scalars(aqua_ctx* x, aqua_scalars* out, void* stream)
+{
+    if (!x || !out)
+        return AQUA_ERR_INVALID;
+    DevScalars hs;
+    AQ_CUDA(cudaMemcpyAsync(&hs, x->sc, sizeof(hs), cudaMemcpyDeviceToHost,
+                            (cudaStream_t)stream));
+    AQ_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    out->t = hs.t;
+    out->dt = hs.dt;
+    out->iter = hs.iter;
+    std::memcpy(out->n_cells, hs.n_cells, sizeof(out->n_cells));
+    std::memcpy(out->r_min, hs.r_min, sizeof(out->r_min));
+    std::memcpy(out->r_max, hs.r_max, sizeof(out->r_max));
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_step(aqua_ctx* x, uint32_t nsteps, int use_graph, void* stream)
+{
+    if (!x || x->N == 0)
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    for (uint32_t k = 0; k < nsteps; k++) {
+        if (!use_graph) {
+            AQ_TRY(enqueue_step(x, x->cur, s));
+        } else {
+            cudaGraphExec_t& g = x->graph[x->cur];
+            if (!g) {
+                cudaGraph_t graph = nullptr;
+                AQ_CUDA(cudaStreamBeginCapture(x->cap_stream,
+                                               cudaStreamCaptureModeThreadLocal));
+                aqua_status st = enqueue_step(x, x->cur, x->cap_stream);
+                cudaError_t e = cudaStreamEndCapture(x->cap_stream, &graph);
+                if (st != AQUA_OK) {
+                    if (graph)
+                        cudaGraphDestroy(graph);
+                    return st;
+                }
+                AQ_CUDA(e);
+                e = cudaGraphInstantiate(&g, graph, 0);
+                cudaGraphDestroy(graph);
+                AQ_CUDA(e);
+            }
+            AQ_CUDA(cudaGraphLaunch(g, s));
+        }
+        x->cur ^= 1;
+    }
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_check(aqua_ctx* x, void* stream)
+{
+    if (!x)
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t err[2] = { 0, 0 };
+    AQ_CUDA(cudaMemcpyAsync(&err[0], &x->sc->err, 4, cudaMemcpyDeviceToHost, s));
+    AQ_CUDA(cudaMemcpyAsync(&err[1], &x->sc_aux->err, 4, cudaMemcpyDeviceToHost, s));
+    AQ_CUDA(cudaStreamSynchronize(s));
+    AQ_CUDA(cudaGetLastError());
+    if (err[0] || err[1]) {
+        const uint32_t zero = 0;
+        AQ_CUDA(cudaMemcpyAsync(&x->sc->err, &zero, 4, cudaMemcpyHostToDevice, s));
+        AQ_CUDA(cudaMemcpyAsync(&x->sc_aux->err, &zero, 4, cudaMemcpyHostToDevice, s));
+        AQ_CUDA(cudaStreamSynchronize(s));
+    }
+    return status_of(err[0] | err[1]);
+}
+
+aqua_status
+aqua_radix_sort(aqua_ctx* x, uint32_t* keys, uint32_t* perm, uint32_t* inv_perm,
+                uint32_t n, uint32_t key_bits, void* stream)
+{
+    if (!x || !keys || n > x->capacity || key_bits > 32)
+        return AQUA_ERR_INVALID;
+    if (n == 0)
+        return AQUA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    StepBufs& b = x->b;
+    const uint32_t passes = sort_passes(key_bits);
+    AQ_CUDA(cudaMemcpyAsync(b.keys[0], keys, n * 4ull, cudaMemcpyDeviceToDevice, s));
+    AQ_CUDA(launch_iota(b.vals[0], n, s));
+    AQ_CUDA(launch_radix_passes(b.keys, b.vals, n, passes, b.counts,
+                                b.digit_total, false, nullptr, s));
+    const int r = passes & 1;
+    AQ_CUDA(cudaMemcpyAsync(keys, b.keys[r], n * 4ull, cudaMemcpyDeviceToDevice, s));
+    if (perm)
+        AQ_CUDA(cudaMemcpyAsync(perm, b.vals[r], n * 4ull, cudaMemcpyDeviceToDevice, s));
+    if (inv_perm)
+        AQ_CUDA(launch_inverse_perm(b.vals[r], inv_perm, n, nullptr, s));
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_linklist(aqua_ctx* x, const float* r_in, uint32_t N, uint32_t* icell,
+              uint32_t* id_sorted, uint32_t* id_unsorted, uint32_t* ihoc,
+              uint32_t ihoc_capacity, uint32_t* n_cells_host,
+              float* r_min_host, float* r_max_host, void* stream)
+{
+    if (!x || !r_in || N == 0 || N > x->capacity || !icell || !ihoc ||
+        ihoc_capacity == 0)
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    StepBufs& b = x->b;
+    const uint32_t ncap = ihoc_capacity < x->ncap ? ihoc_capacity : x->ncap;
+    DevScalars hs;
+    std::memset(&hs, 0, sizeof(hs));
+    AQ_CUDA(cudaMemcpyAsync(x->sc_aux, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(launch_begin(x->sc_aux, b.cells, b.cell_wall, 0, N, s));
+    if (x->dims == 3) {
+        AQ_CUDA(launch_minmax<3>(x->consts, r_in, nullptr, N, x->sc_aux, s));
+        AQ_CUDA(launch_icell_hist<3>(x->consts, r_in, nullptr, N, x->sc_aux,
+                                     ncap, b.keys[0], b.vals[0], b.counts, s));
+    } else {
+        AQ_CUDA(launch_minmax<2>(x->consts, r_in, nullptr, N, x->sc_aux, s));
+        AQ_CUDA(launch_icell_hist<2>(x->consts, r_in, nullptr, N, x->sc_aux,
+                                     ncap, b.keys[0], b.vals[0], b.counts, s));
+    }
+    const uint32_t passes = sort_passes(bits_for(ncap));
+    AQ_CUDA(launch_radix_passes(b.keys, b.vals, N, passes, b.counts,
+                                b.digit_total, true, x->sc_aux, s));
+    const int r = passes & 1;
+    AQ_CUDA(cudaMemcpyAsync(icell, b.keys[r], N * 4ull, cudaMemcpyDeviceToDevice, s));
+    if (id_unsorted)
+        AQ_CUDA(cudaMemcpyAsync(id_unsorted, b.vals[r], N * 4ull,
+                                cudaMemcpyDeviceToDevice, s));
+    if (id_sorted)
+        AQ_CUDA(launch_inverse_perm(b.vals[r], id_sorted, N, x->sc_aux, s));
+    AQ_CUDA(launch_ihoc(b.keys[r], N, ihoc, ncap, x->sc_aux, s));
+    AQ_CUDA(cudaMemcpyAsync(&hs, x->sc_aux, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    AQ_CUDA(cudaStreamSynchronize(s));
+    if (n_cells_host)
+        std::memcpy(n_cells_host, hs.n_cells, sizeof(hs.n_cells));
+    if (r_min_host)
+        std::memcpy(r_min_host, hs.r_min, sizeof(hs.r_min));
+    if (r_max_host)
+        std::memcpy(r_max_host, hs.r_max, sizeof(hs.r_max));
+    if (hs.err) {
+        const uint32_t zero = 0;
+        AQ_CUDA(cudaMemcpyAsync(&x->sc_aux->err, &zero, 4, cudaMemcpyHostToDevice, s));
+        AQ_CUDA(cudaStreamSynchronize(s));
+    }
+    return status_of(hs.err);
+}
+
+aqua_status
+aqua_set_profiling(aqua_ctx* x, int on)
+{
+    if (!x)
+        return AQUA_ERR_INVALID;
+    x->profiling = on ? 1 : 0;
+    drop_graphs(x);
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_stage_times(aqua_ctx* x, float* ms, uint32_t n)
+{
+    if (!x || !ms || n < 4 || !x->profiling)
+        return AQUA_ERR_INVALID;
+    AQ_CUDA(cudaEventSynchronize(x->ev[aqua_ctx::kEvents - 1]));
+    for (int k = 0; k < 4; k++)
+        AQ_CUDA(cudaEventElapsedTime(&ms[k], x->ev[k], x->ev[k + 1]));
+    return AQUA_OK;
+}
+
+uint32_t
+aqua_launches_per_step(aqua_ctx* x)
+{
+    if (!x)
+        return 0;
+    // begin, minmax, icell+hist, (passes - 1) hist, passes x (scan, scatter),
+    // gather, sweep, finalize
+    return 3u + (x->passes - 1u) + 2u * x->passes + 3u;
+}
+
+}  // extern "C"

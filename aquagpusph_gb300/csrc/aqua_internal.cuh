@@ -1,0 +1,113 @@
+// Internal declarations of the aqua_gb300 CUDA library (sm_103a).
+//
+// Floating point contract: the library is compiled with -fmad=false and the
+// default IEEE division / square root, so each multiply, add, divide and
+// square root is one correctly rounded binary32 operation in source order,
+// exactly as the reference's kernels write them (and as the CPU oracle
+// restates them).  Summation order per particle follows the reference's
+// neighbour-visiting order (types/3D.h:197-219: 27 cells, x offset
+// outermost; particles of a cell in sorted order).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/aqua_gb300.h"
+
+namespace aqua {
+
+constexpr int kMaxSets = 16;
+
+// Error word bits written by kernels (read back by aqua_check)
+enum : uint32_t
+{
+    kErrCapacity = 1u << 0,
+    kErrDt = 1u << 1,
+    kErrNonFinite = 1u << 2,
+};
+
+// Case constants as the kernels see them (__constant__ copy per launch set)
+struct Consts
+{
+    int dims;
+    uint32_t n_sets;
+    float h, support, H, CONW, CONF, SUPPORT, DIMS;
+    float cs, p0;
+    float g[4];
+    float courant, dt_Ma, dt_min, dt_fixed;
+    float domain_min[4], domain_max[4];
+    float dr_factor, min_bound_dist, relax_midpoint;
+    uint32_t iter_midpoint_max;
+    float refd[kMaxSets], visc_dyn[kMaxSets], delta[kMaxSets];
+    // derived
+    float cell_length;  // support * h (LinkList.cpp:156)
+    float idist;        // 1 / (support * h) (LinkList.cl.in:73)
+    float q2_reject;    // |r_ij|^2 >= q2_reject  =>  |r_ij| / H >= SUPPORT
+};
+
+// Device-side scalars of the resident state
+struct DevScalars
+{
+    float r_min[4];
+    float r_max[4];
+    uint32_t n_cells[4];
+    float t;
+    float dt;          // time step of the step being run
+    uint32_t dt_next;  // bits of the running minimum of dt_var (atomicMin)
+    uint32_t iter;
+    uint32_t err;      // error bits
+    uint32_t pad[3];
+};
+
+// One set of the per-particle Variables (reference layout)
+struct VarSet
+{
+    uint32_t* id;
+    uint32_t* iset;
+    int32_t* imove;
+    float* r;
+    float* normal;
+    float* tangent;
+    float* binormal;
+    float* u;
+    float* dudt;
+    float* rho;
+    float* drhodt;
+    float* m;
+    float* p;
+};
+
+// Per-step scratch of the link-list and the sweep
+struct StepBufs
+{
+    // link-list
+    uint32_t* keys[2];     // radix ping-pong keys
+    uint32_t* vals[2];     // radix ping-pong values (original index)
+    uint32_t* counts;      // per-pass digit x block counts
+    uint32_t* digit_total; // per-pass digit totals (256)
+    uint2* cells;          // (start, end) per cell; (N, N) if empty
+    uint8_t* cell_wall;    // 1 if the cell holds a boundary element
+    uint32_t* id_sorted;   // old -> new
+    // sorted start-of-step Variables (the reference's *_in after the
+    // midpoint backups)
+    float* r_in;
+    float* u_in;
+    float* dudt_in;
+    float* rho_in;
+    float* drhodt_in;
+    // packed neighbour data (sorted): position + imove, half-step velocity
+    // + density, pressure + mass
+    float4* posq;
+    float4* velq;
+    float2* pmq;
+    // optional intermediates (written when extras are on)
+    float* grad_p;
+    float* lap_u;
+    float* div_u;
+    float* lap_p;
+    float* grad_w_bi;
+    float* div_u_bi;
+    float* shepard;
+};
+
+}  // namespace aqua

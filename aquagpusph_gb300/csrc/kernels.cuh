@@ -1,0 +1,97 @@
+// Kernel-side helpers and launcher declarations shared by the .cu files.
+#pragma once
+
+#include "aqua_internal.cuh"
+
+namespace aqua {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
+
+// The reference's vec type: float4 in 3-D, float2 in 2-D
+template<int D>
+struct Vec;
+template<>
+struct Vec<3>
+{
+    static constexpr int VS = 4;
+    __device__ __forceinline__ static void load(const float* p, uint32_t i, float x[4])
+    {
+        const float4 v = reinterpret_cast<const float4*>(p)[i];
+        x[0] = v.x;
+        x[1] = v.y;
+        x[2] = v.z;
+        x[3] = v.w;
+    }
+    __device__ __forceinline__ static void store(float* p, uint32_t i, const float x[4])
+    {
+        reinterpret_cast<float4*>(p)[i] = make_float4(x[0], x[1], x[2], x[3]);
+    }
+};
+template<>
+struct Vec<2>
+{
+    static constexpr int VS = 2;
+    __device__ __forceinline__ static void load(const float* p, uint32_t i, float x[4])
+    {
+        const float2 v = reinterpret_cast<const float2*>(p)[i];
+        x[0] = v.x;
+        x[1] = v.y;
+        x[2] = 0.f;
+        x[3] = 0.f;
+    }
+    __device__ __forceinline__ static void store(float* p, uint32_t i, const float x[4])
+    {
+        reinterpret_cast<float2*>(p)[i] = make_float2(x[0], x[1]);
+    }
+};
+
+// link-list / sort launchers (linklist.cu)
+cudaError_t launch_begin(DevScalars* sc, uint2* cells, uint8_t* cell_wall,
+                         uint32_t ncap, uint32_t N, cudaStream_t s);
+template<int D>
+cudaError_t launch_minmax(const Consts& c, const float* r, const int32_t* imove,
+                          uint32_t N, DevScalars* sc, cudaStream_t s);
+template<int D>
+cudaError_t launch_icell_hist(const Consts& c, const float* r,
+                              const int32_t* imove, uint32_t N, DevScalars* sc,
+                              uint32_t ncap, uint32_t* keys, uint32_t* vals,
+                              uint32_t* counts, cudaStream_t s);
+cudaError_t launch_radix_passes(uint32_t* keys[2], uint32_t* vals[2],
+                                uint32_t n, uint32_t passes, uint32_t* counts,
+                                uint32_t* digit_total, bool first_counts_ready,
+                                const DevScalars* sc, cudaStream_t s);
+cudaError_t launch_inverse_perm(const uint32_t* perm, uint32_t* inv,
+                                uint32_t n, const DevScalars* sc,
+                                cudaStream_t s);
+cudaError_t launch_ihoc(const uint32_t* keys, uint32_t n, uint32_t* ihoc,
+                        uint32_t ncap, const DevScalars* sc, cudaStream_t s);
+cudaError_t launch_iota(uint32_t* p, uint32_t n, cudaStream_t s);
+uint32_t sort_blocks(uint32_t n);
+uint32_t sort_passes(uint32_t key_bits);
+
+// step launchers (step.cu)
+struct StepArgs
+{
+    uint32_t N;
+    uint32_t ncap;
+    VarSet src;        // previous step's Variables (previous order)
+    VarSet dst;        // this step's Variables (new order)
+    StepBufs b;
+    const uint32_t* skeys;  // sorted cell keys
+    const uint32_t* perm;   // sorted -> previous index
+    DevScalars* sc;
+    int extras;        // write the intermediate operators
+};
+template<int D>
+cudaError_t launch_gather(const Consts& c, const StepArgs& a, cudaStream_t s);
+template<int D>
+cudaError_t launch_sweep(const Consts& c, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_finalize(DevScalars* sc, cudaStream_t s);
+template<int D>
+cudaError_t launch_export_ihoc(const uint2* cells, uint32_t* ihoc,
+                               uint32_t ncap, const DevScalars* sc,
+                               cudaStream_t s);
+
+}  // namespace aqua

@@ -1,0 +1,184 @@
+"""Host-side mirror of the reference's CalcServer for the canonical WCSPH
+step: one resident case on one GPU, advanced by the CUDA library.
+
+The reference builds a CalcServer from the XML presets, registers the
+particle Variables, and calls ``CalcServer::update`` (CalcServer.cpp:592-623)
+to run the tool list once per step.  :class:`Solver` plays that role for the
+tool list this library replaces (include/aqua_gb300.h lists it): it owns the
+library context (device Variables + scratch), loads a :class:`Case`, steps
+it, and reads the Variables back.  All compute goes through
+``libaqua_gb300.so``; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .case import Case, Params
+
+__all__ = ["Solver"]
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
+
+
+class Solver:
+    """A resident case on the current CUDA device."""
+
+    def __init__(self, params: Params, capacity: int, ihoc_capacity: int = 0):
+        self.lib = _lib.load()
+        self.params = params
+        self._pstruct, self._pkeep = _lib.params_struct(params)
+        self.ctx = C.c_void_p()
+        self.ncap = int(ihoc_capacity or params.max_cells())
+        _lib.check("aqua_create", self.lib.aqua_create(
+            C.byref(self._pstruct), int(capacity), self.ncap,
+            C.byref(self.ctx)))
+        self.capacity = int(capacity)
+        self.N = 0
+        self.vs = 4 if params.dims == 3 else 2
+
+    # ------------------------------------------------------------------
+    def close(self):
+        if self.ctx:
+            self.lib.aqua_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_extras(self, on: bool = True):
+        _lib.check("aqua_set_extras", self.lib.aqua_set_extras(self.ctx, int(on)))
+
+    def set_params(self, params: Params):
+        self.params = params
+        self._pstruct, self._pkeep = _lib.params_struct(params)
+        _lib.check("aqua_set_params",
+                   self.lib.aqua_set_params(self.ctx, C.byref(self._pstruct)))
+
+    # ------------------------------------------------------------------
+    def vars_struct(self, arrays: dict) -> _lib.AquaVars:
+        """AquaVars from a dict of host numpy arrays or raw addresses."""
+        v = _lib.AquaVars()
+        for name, typ in _lib.VARS_FIELDS:
+            a = arrays.get(name)
+            if a is None:
+                continue
+            addr = a if isinstance(a, int) else a.ctypes.data
+            setattr(v, name, C.cast(C.c_void_p(addr), typ))
+        return v
+
+    def set_state_raw(self, n, arrays: dict, on_host: bool, t=0.0, dt=0.0,
+                      it=0, stream=None):
+        v = self.vars_struct(arrays)
+        _lib.check("aqua_set_state", self.lib.aqua_set_state(
+            self.ctx, int(n), C.byref(v), int(on_host), float(t), float(dt),
+            int(it), C.c_void_p(stream or 0)))
+        self.N = int(n)
+
+    def get_state_raw(self, arrays: dict, on_host: bool, stream=None):
+        v = self.vars_struct(arrays)
+        _lib.check("aqua_get_state", self.lib.aqua_get_state(
+            self.ctx, C.byref(v), int(on_host), C.c_void_p(stream or 0)))
+
+    def set_case(self, case: Case, stream=None):
+        arrays = {k: np.ascontiguousarray(v) for k, v in case.state_arrays().items()}
+        self._host_in = arrays
+        self.set_state_raw(case.N, arrays, True, case.t, case.dt, case.iter,
+                           stream)
+        self._case = case
+
+    def step(self, n: int = 1, graph: bool = True, stream=None):
+        _lib.check("aqua_step", self.lib.aqua_step(
+            self.ctx, int(n), int(graph), C.c_void_p(stream or 0)))
+
+    def check(self, stream=None):
+        _lib.check("aqua_check", self.lib.aqua_check(self.ctx,
+                                                     C.c_void_p(stream or 0)))
+
+    def scalars(self, stream=None) -> dict:
+        s = _lib.AquaScalars()
+        _lib.check("aqua_get_scalars", self.lib.aqua_get_scalars(
+            self.ctx, C.byref(s), C.c_void_p(stream or 0)))
+        return {"t": s.t, "dt": s.dt, "iter": s.iter,
+                "n_cells": np.array(s.n_cells[:], np.uint32),
+                "r_min": np.array(s.r_min[:], np.float32),
+                "r_max": np.array(s.r_max[:], np.float32)}
+
+    def get_case(self, stream=None) -> Case:
+        """The resident Variables as a host :class:`Case` (synchronises)."""
+        c = Case(self.params, self.N)
+        arrays = c.state_arrays()
+        arrays["shepard"] = np.zeros(self.N, np.float32)
+        self.get_state_raw(arrays, True, stream)
+        sc = self.scalars(stream)
+        c.t, c.dt, c.iter = sc["t"], sc["dt"], sc["iter"]
+        c.shepard = arrays["shepard"]
+        return c
+
+    def get_extra(self, stream=None) -> dict:
+        """Backups, link-list tables and (with extras on) the intermediate
+        operators of the last step, as host arrays (synchronises)."""
+        n, vs = self.N, self.vs
+        sc = self.scalars(stream)
+        vec_names = ("r_in", "u_in", "dudt_in", "grad_p", "lap_u", "grad_w_bi")
+        out = {}
+        for name, typ in _lib.EXTRA_FIELDS:
+            if name == "ihoc":
+                out[name] = np.zeros(self.ncap, np.uint32)
+            elif typ is _lib._U:
+                out[name] = np.zeros(n, np.uint32)
+            elif name in vec_names:
+                out[name] = np.zeros((n, vs), np.float32)
+            else:
+                out[name] = np.zeros(n, np.float32)
+        e = _lib.AquaExtra()
+        for name, typ in _lib.EXTRA_FIELDS:
+            setattr(e, name, C.cast(C.c_void_p(out[name].ctypes.data), typ))
+        _lib.check("aqua_get_extra", self.lib.aqua_get_extra(
+            self.ctx, C.byref(e), 1, C.c_void_p(stream or 0)))
+        self.scalars(stream)
+        out["ihoc"] = out["ihoc"][: int(sc["n_cells"][3])].copy()
+        out.update({k: sc[k] for k in ("n_cells", "r_min", "r_max")})
+        return out
+
+    def linklist(self, r_in: int, n: int, icell: int, id_sorted: int,
+                 id_unsorted: int, ihoc: int, ihoc_capacity: int,
+                 stream=None) -> dict:
+        """The link-list tool on caller device buffers (addresses)."""
+        nc = (C.c_uint32 * 4)()
+        mn = (C.c_float * 4)()
+        mx = (C.c_float * 4)()
+        _lib.check("aqua_linklist", self.lib.aqua_linklist(
+            self.ctx, C.c_void_p(r_in), int(n), C.c_void_p(icell),
+            C.c_void_p(id_sorted), C.c_void_p(id_unsorted), C.c_void_p(ihoc),
+            int(ihoc_capacity), nc, mn, mx, C.c_void_p(stream or 0)))
+        return {"n_cells": np.array(nc[:], np.uint32),
+                "r_min": np.array(mn[:], np.float32),
+                "r_max": np.array(mx[:], np.float32)}
+
+    def radix_sort(self, keys: int, perm: int, inv_perm: int, n: int,
+                   key_bits: int, stream=None):
+        """The radix-sort tool on caller device buffers (addresses)."""
+        _lib.check("aqua_radix_sort", self.lib.aqua_radix_sort(
+            self.ctx, C.c_void_p(keys), C.c_void_p(perm), C.c_void_p(inv_perm),
+            int(n), int(key_bits), C.c_void_p(stream or 0)))
+
+    def set_profiling(self, on: bool = True):
+        _lib.check("aqua_set_profiling",
+                   self.lib.aqua_set_profiling(self.ctx, int(on)))
+
+    def stage_times(self) -> dict:
+        """Milliseconds of the stages of the last step (profiling on)."""
+        ms = (C.c_float * 4)()
+        _lib.check("aqua_stage_times", self.lib.aqua_stage_times(self.ctx, ms, 4))
+        return dict(zip(("linklist", "gather", "sweep", "finalize"), ms[:]))
+
+    def launches_per_step(self) -> int:
+        return int(self.lib.aqua_launches_per_step(self.ctx))

@@ -1,0 +1,374 @@
+"""Benchmark: particle-steps/s of the canonical WCSPH step on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c1|c0] [--no-cpu-baseline]
+
+Workload (default c1): the 3-D dam break, SPHERIC test-2 tank 3.22 x 1.0 x
+1.0 m, water block 1.228 x 1.0 x 0.55 m on a dx = 0.005 m lattice (5,412,000
+fluid particles), boundary-integral elements at dx on the five walls
+(466,400), 4 pressure probes: N = 5,878,404.  h = 2 dx, Wendland, c0 = 40,
+linear EOS, delta-SPH 0.1, Morris viscosity nu = 1e-6, midpoint scheme, CFL
+0.1.  Synthetic inputs built by aquagpusph_gb300.case.dam_break_3d().
+
+A step is one full canonical step (link-list + sort + gather + fused sweep
++ integrator + dt), replayed from a CUDA graph.  The resident state (~2.5 GB)
+is far larger than the 129 MB L2, so no flush is needed between steps.
+
+One JSON line is printed by rank 0.  Multi-GPU runs (torchrun) are
+independent replicas of the workload, one per GPU (the step has no exchange
+between GPUs); value aggregates all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (canonical WCSPH step, 1 GB300)"
+UNIT = "particle-steps/s"
+
+# Algorithmic bytes per particle (3-D, V = 16 B):
+#   whole step  B = 19 V + 96 + 20 P (P = 3 radix passes)     = 460 B
+#   fused sweep = SURVEY rows S5 + S6: read r,u,rho,m,imove,normal (3V+12),
+#                 write dudt,drhodt (V+4); read r,u,rho,dudt,drhodt (3V+8),
+#                 write r,u,rho (2V+4)                          = 9V + 28
+STEP_BYTES_3D = 19 * 16 + 96 + 20 * 3
+SWEEP_BYTES_3D = 9 * 16 + 28
+STEP_BYTES_2D = 19 * 8 + 96 + 20 * 2
+SWEEP_BYTES_2D = 9 * 8 + 28
+
+
+def workload(name):
+    from aquagpusph_gb300 import case as cases
+    if name == "c0":
+        c = cases.dam_break_2d()
+        desc = ("2-D dam break, tank 3.22x1.8 m, column 1.2x0.6 m, dx=0.01 m, "
+                f"h=0.02 m, c0=45, BIe walls, 1 probe: N={c.N}")
+    else:
+        c = cases.dam_break_3d()
+        desc = ("3-D dam break, SPHERIC test-2 tank 3.22x1.0x1.0 m, block "
+                "1.228x1.0x0.55 m, dx=0.005 m, h=0.01 m, c0=40, BIe walls on "
+                f"5 faces, 4 probes: N={c.N}")
+    c.dt = c.params.dt_fixed
+    return c, desc
+
+
+def cpu_sample(name):
+    """A bounded sample of the workload for the CPU runs: the same lattice,
+    smoothing length, constants and wall treatment on a smaller tank."""
+    from aquagpusph_gb300 import case as cases
+    if name == "c0":
+        c = cases.dam_break_2d()
+        desc = f"the full 2-D dam break (N={c.N})"
+    else:
+        c = cases.dam_break_3d(tank=(0.8, 0.2, 0.6), block=(0.4, 0.2, 0.55),
+                               probes_z=(0.02, 0.06))
+        desc = ("3-D dam break slab at the workload's dx=0.005 m / h=0.01 m: "
+                f"tank 0.8x0.2x0.6 m, block 0.4x0.2x0.55 m, N={c.N}")
+    c.dt = c.params.dt_fixed
+    return c, desc
+
+
+def time_oracle(c, steps, warmup):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    orc = O.load_oracle()
+    st = O.OracleState(c)
+    nt = os.cpu_count() or 1
+    orc.step(st, nthreads=nt, steps=max(warmup, 0))
+    t0 = time.perf_counter()
+    orc.step(st, nthreads=nt, steps=steps)
+    dt = time.perf_counter() - t0
+    return c.N * steps / dt, nt, dt
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def load_traffic(kernel):
+    """Per-particle DRAM bytes of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    c, desc = cpu_sample(args.workload)
+    value, nt, secs = time_oracle(c, args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_desc(args.workload), "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt,
+                         "kind": "port",
+                         "sample": desc + "; the CPU oracle (C++ restatement of "
+                         "the reference kernels, OpenMP over particles)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_desc(name):
+    from aquagpusph_gb300 import case as cases
+    if name == "c0":
+        return "2-D dam break (N=8,205)"
+    return "3-D dam break, SPHERIC test-2 geometry, dx=0.005 m (N=5,878,404)"
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from aquagpusph_gb300 import _lib
+    from aquagpusph_gb300.solver import Solver
+
+    c, desc = workload(args.workload)
+    three_d = c.dims == 3
+    sv = Solver(c.params, capacity=c.N)
+    sv.set_case(c)
+    stream = torch.cuda.Stream()
+    sid = stream.cuda_stream
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    with torch.cuda.stream(stream):
+        sv.step(max(args.warmup, 3), graph=True, stream=sid)
+    stream.synchronize()
+    sv.check(stream=sid)
+
+    # ---- timed region: K steps replayed from the CUDA graphs
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    sv.step(args.steps, graph=True, stream=sid)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    sv.check(stream=sid)
+    sc = sv.scalars(stream=sid)
+    ms_step = ms_total / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+        ms_step = ms_total / args.steps
+    value = world * c.N * args.steps / (ms_total * 1e-3)
+
+    # ---- per-stage CUDA events (same graphs with event nodes), K steps
+    sv.set_profiling(True)
+    stage = {"linklist": [], "gather": [], "sweep": [], "finalize": []}
+    for _ in range(args.steps):
+        sv.step(1, graph=True, stream=sid)
+        for k, v in sv.stage_times().items():
+            stage[k].append(v)
+    sv.set_profiling(False)
+    sv.check(stream=sid)
+    stage_ms = {k: float(np.mean(v)) for k, v in stage.items()}
+    top = max(stage_ms, key=stage_ms.get)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    host = {}
+    for name, a in c.state_arrays().items():
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:] = np.ascontiguousarray(a).view(np.uint8).ravel()
+        host[name] = t
+    out = {name: torch.empty_like(t, pin_memory=True) for name, t in host.items()}
+    addr_in = {k: t.data_ptr() for k, t in host.items()}
+    addr_out = {k: t.data_ptr() for k, t in out.items()}
+    h2d = sum(t.numel() for t in host.values())
+    d2h = sum(t.numel() for t in out.values())
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sv.set_state_raw(c.N, addr_in, True, c.t, c.dt, c.iter, stream=sid)
+        sv.step(1, graph=True, stream=sid)
+        sv.get_state_raw(addr_out, True, stream=sid)
+    stream.synchronize()
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    sv.check(stream=sid)
+    e2e_value = world * c.N * e2e_steps / e2e_s
+
+    # ---- roofline of the dominant kernel (the fused sweep)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    sweep_b = SWEEP_BYTES_3D if three_d else SWEEP_BYTES_2D
+    step_b = STEP_BYTES_3D if three_d else STEP_BYTES_2D
+    achieved = sweep_b * c.N / (stage_ms["sweep"] * 1e-3) / 1e9
+    traffic_pp = load_traffic("k_sweep<3>" if three_d else "k_sweep<2>")
+    roofline = {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_src,
+                "traffic": traffic_pp * c.N if traffic_pp else None,
+                "algorithmic_bytes_per_launch": sweep_b * c.N}
+    step_achieved = step_b * c.N / (ms_step * 1e-3) / 1e9
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            cs, sdesc = cpu_sample(args.workload)
+            v, nt, secs = time_oracle(cs, args.cpu_steps, 1)
+            cpu = {"value": v, "unit": UNIT, "cores": nt, "kind": "port",
+                   "sample": f"{sdesc}, {args.cpu_steps} steps in {secs:.1f} s "
+                             "(CPU oracle: C++ restatement of the reference "
+                             "kernels, OpenMP over particles)"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (resident state ~"
+                             f"{sv.capacity * 430 / 1e9:.1f} GB)",
+                       "cuda_graph": True, "precision": "IEEE f32, no FMA "
+                       "contraction (bit-exact with the oracle)"},
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps},
+            "gpu_launches": sv.launches_per_step() * args.steps,
+            "roofline": roofline,
+            "step_roofline": {"bound": "hbm", "achieved": step_achieved,
+                              "peak": peak, "unit": "GB/s",
+                              "frac": step_achieved / peak,
+                              "algorithmic_bytes_per_particle_step": step_b},
+            "stage_ms": stage_ms, "dominant_stage": top,
+            "cpu_baseline": cpu, "clocks": clk,
+            "sim": {"t": sc["t"], "dt": sc["dt"], "iter": sc["iter"],
+                    "n_cells": [int(x) for x in sc["n_cells"]]},
+        }
+        print(json.dumps(line), flush=True)
+    sv.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,228 @@
+/*
+ * aqua_gb300 -- GB300 (sm_103a) CUDA implementation of AQUAgpusph's per-step
+ * WCSPH particle pipeline, behind a plain C ABI.
+ *
+ * The reference runs the step as a list of OpenCL tools configured by XML
+ * presets (basic.xml:132-171 plus the midpoint, domain, cfd, deltaSPH, BIe
+ * and variableTimeStep presets).  This library replaces the tools of that
+ * path:
+ *
+ *   reference tool(s)                                   entry point here
+ *   --------------------------------------------------  --------------------
+ *   link-list (LinkList.cpp:326-494: Reduction min/max,  aqua_linklist()
+ *     nCells, iCell, RadixSort, iHoc, linkList)
+ *   radix-sort (RadixSort.cpp:130-304)                   aqua_radix_sort()
+ *   predictor, Domain, link-list, Backup*, sort stage1/2, aqua_step()
+ *     EOS, Binormal, reinit sets, midpoint loop (advance,
+ *     eos, cfd Shepard/interactions/sensors/lap p, BIe
+ *     interactions/rates, cfd rates, delta-SPH, elastic
+ *     bounce, relax), corrector, BIe pst, time step,
+ *     minimum time step reduction, t += dt
+ *
+ * Conventions
+ *   - extern "C", POD arguments only; no exception crosses the ABI.
+ *   - every function returns an aqua_status (0 = success, negative = error).
+ *   - device pointers unless a name says "host".
+ *   - `vec` arrays hold float4 per particle in 3-D and float2 in 2-D (the
+ *     reference's vec type); index arrays are uint32 (the reference's usize
+ *     on 32-bit-address devices, CalcServer.cpp:260-264).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy stream).
+ *   - A context lives on the device that was current at aqua_create().
+ */
+#ifndef AQUA_GB300_H
+#define AQUA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum
+{
+    AQUA_OK = 0,
+    AQUA_ERR_INVALID = -1,     /* bad argument */
+    AQUA_ERR_CAPACITY = -2,    /* n_cells exceeds the ihoc capacity */
+    AQUA_ERR_DT = -3,          /* time step not > 0 (variableTimeStep.xml:16) */
+    AQUA_ERR_CUDA = -4,        /* a CUDA runtime call failed */
+    AQUA_ERR_NO_MEMORY = -5,   /* device allocation failed */
+    AQUA_ERR_NONFINITE = -6    /* non-finite position reached the link-list */
+} aqua_status;
+
+/* Scalar Variables and Definitions of one case.  The Definitions are the
+ * compiled values: CalcServer.cpp:247-257 bakes evaluated expressions in as
+ * "%#G" literals, so H, CONW, CONF and DIMS carry six significant digits. */
+typedef struct
+{
+    int32_t dims;              /* 2 or 3 */
+    uint32_t n_sets;           /* length of refd / visc_dyn / delta */
+    float h;                   /* Variable h */
+    float support;             /* Variable support (kernel support / h) */
+    float H;                   /* Definition H */
+    float CONW;                /* Definition CONW = 1/h^dims */
+    float CONF;                /* Definition CONF = 1/h^(dims+2) */
+    float SUPPORT;             /* Definition SUPPORT */
+    float DIMS;                /* Definition DIMS */
+    float cs;                  /* Variable cs (speed of sound) */
+    float p0;                  /* Variable p0 (background pressure) */
+    float g[4];                /* Variable g (gravity) */
+    float courant;             /* Variable courant */
+    float dt_Ma;               /* Variable dt_Ma */
+    float dt_min;              /* Variable dt_min */
+    float dt_fixed;            /* "fixed time step" = courant*h/cs */
+    float domain_min[4];       /* Variable domain_min */
+    float domain_max[4];       /* Variable domain_max */
+    float dr_factor;           /* Definition __DR_FACTOR__ */
+    float min_bound_dist;      /* Definition __MIN_BOUND_DIST__ */
+    float relax_midpoint;      /* Variable relax_midpoint */
+    uint32_t iter_midpoint_max; /* Variable iter_midpoint_max */
+    const float* refd;         /* host, n_sets: per-set reference density */
+    const float* visc_dyn;     /* host, n_sets: dynamic viscosity */
+    const float* delta;        /* host, n_sets: delta-SPH factor */
+} aqua_params;
+
+/* The particle Variables of one case (all length N; pointers may be host or
+ * device memory as each function states).  Fields a call does not use may
+ * be NULL. */
+typedef struct
+{
+    uint32_t* id;
+    uint32_t* iset;
+    int32_t* imove;
+    float* r;          /* vec */
+    float* normal;     /* vec */
+    float* tangent;    /* vec */
+    float* binormal;   /* vec */
+    float* u;          /* vec */
+    float* dudt;       /* vec */
+    float* rho;
+    float* drhodt;
+    float* m;
+    float* p;
+    float* shepard;
+} aqua_vars;
+
+/* Variables a step leaves behind besides the state (the reference keeps
+ * them as Variables too): backups, link-list tables and the step's
+ * intermediate operators.  Used by aqua_get_extra(). */
+typedef struct
+{
+    float* r_in;       /* vec, sorted start-of-step positions */
+    float* u_in;       /* vec */
+    float* dudt_in;    /* vec */
+    float* rho_in;
+    float* drhodt_in;
+    uint32_t* icell;   /* sorted cell of each particle */
+    uint32_t* id_sorted;   /* old index -> sorted index */
+    uint32_t* id_unsorted; /* sorted index -> old index */
+    uint32_t* ihoc;    /* head of chain of each cell, N if empty (n_cells.w) */
+    float* grad_p;     /* vec, after the BIe rates */
+    float* lap_u;      /* vec */
+    float* div_u;      /* after the BIe rates */
+    float* lap_p;
+    float* grad_w_bi;  /* vec */
+    float* div_u_bi;
+} aqua_extra;
+
+/* Scalars of the resident state */
+typedef struct
+{
+    float t;
+    float dt;
+    uint32_t iter;
+    uint32_t n_cells[4];
+    float r_min[4];
+    float r_max[4];
+} aqua_scalars;
+
+typedef struct aqua_ctx aqua_ctx;
+
+/* Library version string */
+const char* aqua_version(void);
+
+/* Creates a context for cases of up to `capacity` particles on the current
+ * device.  `ihoc_capacity` bounds n_cells.w (0 = derive it from the domain
+ * box in `params`).  Allocates all device memory the step needs; no later
+ * call allocates.  (CalcServer::setup, CalcServer.cpp:1435-1534, and
+ * LinkList::setup / allocate, LinkList.cpp:137-183, 234-271.) */
+aqua_status aqua_create(const aqua_params* params, uint32_t capacity,
+                        uint32_t ihoc_capacity, aqua_ctx** out);
+aqua_status aqua_destroy(aqua_ctx* ctx);
+
+/* Replaces the case parameters (same dims and ihoc capacity). */
+aqua_status aqua_set_params(aqua_ctx* ctx, const aqua_params* params);
+
+/* With `on` = 1 every step also stores the intermediate operators (grad_p,
+ * lap_u, div_u, lap_p, grad_w_bi, div_u_bi) the reference keeps as
+ * Variables, for aqua_get_extra(); off by default (the fused step does not
+ * need them). */
+aqua_status aqua_set_extras(aqua_ctx* ctx, int on);
+
+/* Uploads the particle Variables of an N-particle case into the resident
+ * state (the ParticlesSet loaders, FileManager.cpp:136-139).  `on_host` = 1
+ * for host pointers (pinned memory makes the copies asynchronous), 0 for
+ * device pointers.  Required fields: id, iset, imove, r, normal, tangent, u,
+ * dudt, rho, drhodt, m, p.  binormal may be NULL.  Also sets t, dt, iter. */
+aqua_status aqua_set_state(aqua_ctx* ctx, uint32_t N, const aqua_vars* src,
+                           int on_host, float t, float dt, uint32_t iter,
+                           void* stream);
+
+/* Copies the resident state out (any non-NULL field is written). */
+aqua_status aqua_get_state(aqua_ctx* ctx, aqua_vars* dst, int on_host,
+                           void* stream);
+aqua_status aqua_get_extra(aqua_ctx* ctx, aqua_extra* dst, int on_host,
+                           void* stream);
+/* Synchronises `stream` and reads the scalars. */
+aqua_status aqua_get_scalars(aqua_ctx* ctx, aqua_scalars* out, void* stream);
+
+/* Advances the resident state by `nsteps` full canonical steps (the tool
+ * list of CalcServer::update, CalcServer.cpp:592-623, for one step each).
+ * Launch-only: no host synchronisation; dt stays on the device.  With
+ * `use_graph` = 1 the step is captured once into a CUDA graph per parity
+ * of the step and replayed. */
+aqua_status aqua_step(aqua_ctx* ctx, uint32_t nsteps, int use_graph,
+                      void* stream);
+
+/* Synchronises `stream` and returns the first error a kernel recorded since
+ * the last call (AQUA_ERR_CAPACITY, AQUA_ERR_DT, AQUA_ERR_NONFINITE), then
+ * clears it.  The step skips its remaining work once an error is set. */
+aqua_status aqua_check(aqua_ctx* ctx, void* stream);
+
+/* The link-list tool on caller-owned device buffers (LinkList.cpp:326-494):
+ * r_min/r_max of r_in over all N particles, n_cells = floor((max - min) /
+ * (support*h)) + 6 per axis, icell of every particle, a stable sort of icell
+ * (id_unsorted[s] = original index, id_sorted[orig] = s) and ihoc (N for an
+ * empty cell).  Outputs: icell (N, sorted), id_sorted (N), id_unsorted (N),
+ * ihoc (ihoc_capacity; n_cells.w entries written), host n_cells[4],
+ * r_min[4], r_max[4].  Synchronises `stream` once (the reference's
+ * LinkList also waits for its reductions, LinkList.cpp:350-356). */
+aqua_status aqua_linklist(aqua_ctx* ctx, const float* r_in, uint32_t N,
+                          uint32_t* icell, uint32_t* id_sorted,
+                          uint32_t* id_unsorted, uint32_t* ihoc,
+                          uint32_t ihoc_capacity, uint32_t* n_cells_host,
+                          float* r_min_host, float* r_max_host,
+                          void* stream);
+
+/* The radix-sort tool on caller device buffers (RadixSort.cpp:130-304):
+ * stable ascending sort of n keys below 2^key_bits (keys sorted in place),
+ * perm[s] = original index, inv_perm[orig] = s (either may be NULL). */
+aqua_status aqua_radix_sort(aqua_ctx* ctx, uint32_t* keys, uint32_t* perm,
+                            uint32_t* inv_perm, uint32_t n, uint32_t key_bits,
+                            void* stream);
+
+/* With `on` = 1 each step records CUDA events at its stage boundaries (also
+ * inside captured graphs); aqua_stage_times() then returns, for the last
+ * step, the milliseconds of [0] link-list (bounding box, hash, sort),
+ * [1] gather, [2] sweep, [3] finalize.  Profiling plays the role of the
+ * reference's per-tool EventProfile (Kernel.cpp:38-116). */
+aqua_status aqua_set_profiling(aqua_ctx* ctx, int on);
+aqua_status aqua_stage_times(aqua_ctx* ctx, float* ms, uint32_t n);
+
+/* Number of kernel launches one aqua_step() step issues (for accounting). */
+uint32_t aqua_launches_per_step(aqua_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

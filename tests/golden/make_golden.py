@@ -1,0 +1,118 @@
+"""Generates the golden fixtures of tests/golden/ (run where the reference
+tree is mounted; the fixtures are committed so that hosts without it, the
+GPU host included, can check against them).
+
+    python tests/golden/make_golden.py [/path/to/reference]
+
+* linklist_{2d,3d}.npz -- the reference's LinkList test input
+  (tests/{2D,3D}/LinkList/cMake/particles.dat, loaded twice as two particle
+  sets of 500, h = 0.1, support = 2, as tests/*/LinkList/cMake/main.xml
+  does) and the link-list the reference's own iCell/iHoc/linkList kernels
+  give on it (oracle/_ref harness): icell, id_sorted, id_unsorted, ihoc,
+  n_cells, r_min, r_max.
+* radixsort_3d.npz -- the keys of tests/3D/RadixSort/cMake/particles.dat
+  (5th column) and their stable sort: sorted keys, perm, inv_perm.
+* step_{2d,3d}.npz -- a small perturbed dam break (every particle type, a
+  NaN and an out-of-domain particle, random velocities and rates) and the
+  Variables after two canonical steps of the reference-kernel harness.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from aquagpusph_gb300 import case as cases  # noqa: E402
+import oracle as O  # noqa: E402
+sys.path.insert(0, HERE)
+from golden_cases import perturbed, small_case  # noqa: E402
+
+STATE_KEYS = ("id", "iset", "imove", "r", "normal", "tangent", "binormal",
+              "u", "dudt", "rho", "drhodt", "m", "p")
+
+
+def read_columns(path):
+    rows = []
+    with open(path) as f:
+        for line in f:
+            line = line.replace(",", " ").strip()
+            if line:
+                rows.append([float(x) for x in line.split()])
+    return np.array(rows)
+
+
+def linklist_case(dims, pos):
+    vs = 4 if dims == 3 else 2
+    p = cases.Params(dims=dims, h=0.1, cs=1.0, g=(0, 0, 0, 0),
+                     refd=(1.0, 1.0), visc_dyn=(0.0, 0.0), delta=(0.0, 0.0),
+                     domain_min=(-10, -10, -10, 0), domain_max=(10, 10, 10, 0))
+    n = 2 * len(pos)
+    c = cases.Case(p, n)
+    c.r[:, :] = 0
+    c.r[: len(pos), :dims] = pos[:, :dims]
+    c.r[len(pos):, :dims] = pos[:, :dims]
+    c.iset[len(pos):] = 1
+    return c
+
+
+def make_linklist(ref_root):
+    out = {}
+    for dims in (2, 3):
+        pos = read_columns(os.path.join(ref_root, "tests", f"{dims}D", "LinkList",
+                                        "cMake", "particles.dat"))
+        c = linklist_case(dims, pos.astype(np.float32))
+        lib = O.load_ref(dims)
+        st = O.OracleState(c, ihoc_capacity=1 << 16)
+        st.arrays["r_in"][...] = c.r
+        lib.linklist(st)
+        out[dims] = dict(r=c.r, h=np.float32(0.1), support=np.float32(2.0),
+                         icell=st["icell"], id_sorted=st["id_sorted"],
+                         id_unsorted=st["id_unsorted"], ihoc=st["ihoc"],
+                         n_cells=st["n_cells"], r_min=st["r_min"],
+                         r_max=st["r_max"])
+        np.savez_compressed(os.path.join(HERE, f"linklist_{dims}d.npz"),
+                            **out[dims])
+    return out
+
+
+def make_radixsort(ref_root):
+    data = read_columns(os.path.join(ref_root, "tests", "3D", "RadixSort",
+                                     "cMake", "particles.dat"))
+    keys = data[:, 4].astype(np.uint32)
+    k, perm, inv = O.load_ref(3).sort(keys)
+    np.savez_compressed(os.path.join(HERE, "radixsort_3d.npz"), keys=keys,
+                        sorted=k, perm=perm, inv_perm=inv)
+
+
+def make_steps():
+    for dims in (2, 3):
+        c = perturbed(small_case(dims), 11 + dims)
+        st = O.OracleState(c)
+        O.load_ref(dims).step(st, steps=2)
+        data = {"in_" + k: getattr(c, k) for k in STATE_KEYS}
+        data.update({"in_t": np.float32(c.t), "in_dt": np.float32(c.dt),
+                     "in_iter": np.uint32(c.iter)})
+        for k, a in st.arrays.items():
+            data["out_" + k] = st[k] if k == "ihoc" else a
+        for k in ("n_cells", "r_min", "r_max", "t", "dt", "iter"):
+            data["out_" + k] = np.asarray(st[k])
+        np.savez_compressed(os.path.join(HERE, f"step_{dims}d.npz"), **data)
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    O.build_oracle(ref=True)
+    make_linklist(ref_root)
+    make_radixsort(ref_root)
+    make_steps()
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()
