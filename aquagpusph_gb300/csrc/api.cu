@@ -213,7 +213,7 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     StepBufs& b = x->b;
     const uint32_t N = x->N;
     if (x->profiling)
-        AQ_CUDA(cudaEventRecord(x->ev[0], s));
+        AQ_CUDA(cudaEventRecordWithFlags(x->ev[0], s, cudaEventRecordExternal));
     AQ_CUDA(launch_begin(x->sc, b.cells, b.cell_wall, x->ncap, N, s));
     if (x->dims == 3) {
         AQ_CUDA(launch_minmax<3>(x->consts, S.r, S.imove, N, x->sc, s));
@@ -237,22 +237,22 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     a.sc = x->sc;
     a.extras = x->extras;
     if (x->profiling)
-        AQ_CUDA(cudaEventRecord(x->ev[1], s));
+        AQ_CUDA(cudaEventRecordWithFlags(x->ev[1], s, cudaEventRecordExternal));
     if (x->dims == 3)
         AQ_CUDA(launch_gather<3>(x->consts, a, s));
     else
         AQ_CUDA(launch_gather<2>(x->consts, a, s));
     if (x->profiling)
-        AQ_CUDA(cudaEventRecord(x->ev[2], s));
+        AQ_CUDA(cudaEventRecordWithFlags(x->ev[2], s, cudaEventRecordExternal));
     if (x->dims == 3)
         AQ_CUDA(launch_sweep<3>(x->consts, a, s));
     else
         AQ_CUDA(launch_sweep<2>(x->consts, a, s));
     if (x->profiling)
-        AQ_CUDA(cudaEventRecord(x->ev[3], s));
+        AQ_CUDA(cudaEventRecordWithFlags(x->ev[3], s, cudaEventRecordExternal));
     AQ_CUDA(launch_finalize(x->sc, s));
     if (x->profiling)
-        AQ_CUDA(cudaEventRecord(x->ev[4], s));
+        AQ_CUDA(cudaEventRecordWithFlags(x->ev[4], s, cudaEventRecordExternal));
     return AQUA_OK;
 }
 

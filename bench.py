@@ -51,6 +51,17 @@ SWEEP_BYTES_2D = 9 * 8 + 28
 
 def workload(name):
     from aquagpusph_gb300 import case as cases
+    if name == "c1s":
+        c, _ = cpu_sample("c1")
+        return c, ("3-D dam break slab at dx=0.005 m, h=0.01 m (tank "
+                   f"0.8x0.2x0.6 m, block 0.4x0.2x0.55 m): N={c.N}")
+    if name == "c1m":
+        # profiling size: same lattice, state (~0.8 GB) well above the L2
+        c = cases.dam_break_3d(tank=(1.6, 0.5, 0.6), block=(0.8, 0.5, 0.55),
+                               probes_z=(0.02, 0.06))
+        c.dt = c.params.dt_fixed
+        return c, ("3-D dam break at dx=0.005 m, h=0.01 m (tank 1.6x0.5x0.6 m, "
+                   f"block 0.8x0.5x0.55 m): N={c.N}")
     if name == "c0":
         c = cases.dam_break_2d()
         desc = ("2-D dam break, tank 3.22x1.8 m, column 1.2x0.6 m, dx=0.01 m, "
@@ -68,6 +79,8 @@ def cpu_sample(name):
     """A bounded sample of the workload for the CPU runs: the same lattice,
     smoothing length, constants and wall treatment on a smaller tank."""
     from aquagpusph_gb300 import case as cases
+    if name in ("c1s", "c1m"):
+        name = "c1"
     if name == "c0":
         c = cases.dam_break_2d()
         desc = f"the full 2-D dam break (N={c.N})"
@@ -189,7 +202,10 @@ def run_reference(args):
 
 
 def workload_desc(name):
-    from aquagpusph_gb300 import case as cases
+    if name == "c1m":
+        return "3-D dam break, 1.6x0.5x0.6 m tank, dx=0.005 m"
+    if name == "c1s":
+        return "3-D dam break slab, dx=0.005 m"
     if name == "c0":
         return "2-D dam break (N=8,205)"
     return "3-D dam break, SPHERIC test-2 geometry, dx=0.005 m (N=5,878,404)"
@@ -359,7 +375,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c1s", "c1m"])
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

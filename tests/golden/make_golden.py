@@ -14,7 +14,8 @@ GPU host included, can check against them).
   (5th column) and their stable sort: sorted keys, perm, inv_perm.
 * step_{2d,3d}.npz -- a small perturbed dam break (every particle type, a
   NaN and an out-of-domain particle, random velocities and rates) and the
-  Variables after two canonical steps of the reference-kernel harness.
+  Variables after one (out1_*) and two (out2_*) canonical steps of the
+  reference-kernel harness.
 """
 import os
 import sys
@@ -92,14 +93,16 @@ def make_steps():
     for dims in (2, 3):
         c = perturbed(small_case(dims), 11 + dims)
         st = O.OracleState(c)
-        O.load_ref(dims).step(st, steps=2)
         data = {"in_" + k: getattr(c, k) for k in STATE_KEYS}
         data.update({"in_t": np.float32(c.t), "in_dt": np.float32(c.dt),
                      "in_iter": np.uint32(c.iter)})
-        for k, a in st.arrays.items():
-            data["out_" + k] = st[k] if k == "ihoc" else a
-        for k in ("n_cells", "r_min", "r_max", "t", "dt", "iter"):
-            data["out_" + k] = np.asarray(st[k])
+        lib = O.load_ref(dims)
+        for step in (1, 2):
+            lib.step(st)
+            for k, a in st.arrays.items():
+                data[f"out{step}_" + k] = (st[k] if k == "ihoc" else a).copy()
+            for k in ("n_cells", "r_min", "r_max", "t", "dt", "iter"):
+                data[f"out{step}_" + k] = np.asarray(st[k])
         np.savez_compressed(os.path.join(HERE, f"step_{dims}d.npz"), **data)
 
 
