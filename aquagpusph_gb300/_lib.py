@@ -22,6 +22,9 @@ AQUA_ERR_CUDA = -4
 AQUA_ERR_NO_MEMORY = -5
 AQUA_ERR_NONFINITE = -6
 
+AQUA_PRECISION_EXACT = 0
+AQUA_PRECISION_FAST = 1
+
 STATUS_NAMES = {
     AQUA_OK: "AQUA_OK",
     AQUA_ERR_INVALID: "AQUA_ERR_INVALID",
@@ -92,6 +95,7 @@ SIGNATURES = [
     ("aqua_destroy", C.c_int, [C.c_void_p]),
     ("aqua_set_params", C.c_int, [C.c_void_p, C.POINTER(AquaParams)]),
     ("aqua_set_extras", C.c_int, [C.c_void_p, C.c_int]),
+    ("aqua_set_precision", C.c_int, [C.c_void_p, C.c_int]),
     ("aqua_set_state", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(AquaVars),
                                  C.c_int, C.c_float, C.c_float, C.c_uint32,
                                  C.c_void_p]),

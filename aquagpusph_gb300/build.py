@@ -21,7 +21,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libaqua_gb300.so")
-SOURCES = ("linklist.cu", "step.cu", "api.cu")
+SOURCES = ("linklist.cu", "step.cu", "step_fast.cu", "api.cu")
+# per-file arithmetic: the fast step kernels trade the reference's exact
+# rounding for FMA contraction and approximate division / square root
+FAST_MATH = {"step_fast.cu"}
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -34,9 +37,10 @@ def nvcc() -> str:
                        "aquagpusph_gb300")
 
 
-def _flags():
-    return [ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
-            "-Xcompiler", "-fPIC", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
+def _flags(src=""):
+    math = ["-use_fast_math"] if src in FAST_MATH else ["-fmad=false"]
+    return [ARCH, "-O3", "-lineinfo", "-std=c++17"] + math + [
+        "-Xcompiler", "-fPIC", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
 
 
 def _stale(target, deps):
@@ -60,7 +64,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         o = os.path.join(objdir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([cc] + _flags() + ["-c", s, "-o", o])
+            jobs.append([cc] + _flags(src) + ["-c", s, "-o", o])
 
     def run(cmd):
         if verbose:

@@ -31,6 +31,8 @@ struct aqua_ctx
     DevScalars* sc_aux = nullptr;  // standalone link-list / sort
     uint32_t* ihoc_out = nullptr;  // ihoc export buffer (ncap)
     int extras = 0;
+    int fast = 0;              // 1: -use_fast_math step kernels
+    unsigned sweep_grid = 0;   // persistent sweep blocks
     void* pool = nullptr;
     size_t pool_bytes = 0;
     cudaStream_t cap_stream = nullptr;
@@ -170,6 +172,7 @@ layout(aqua_ctx* x, char* base)
     b.counts = cv.take<uint32_t>((size_t)256 * nb);
     b.digit_total = cv.take<uint32_t>(256);
     b.cells = cv.take<uint2>(x->ncap);
+    b.chunks = cv.take<uint2>(n);
     b.cell_wall = cv.take<uint8_t>(x->ncap);
     b.id_sorted = cv.take<uint32_t>(n);
     b.r_in = cv.take<float>((size_t)n * VS);
@@ -239,15 +242,15 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[1], s, cudaEventRecordExternal));
     if (x->dims == 3)
-        AQ_CUDA(launch_gather<3>(x->consts, a, s));
+        AQ_CUDA(launch_gather<3>(x->fast, x->consts, a, s));
     else
-        AQ_CUDA(launch_gather<2>(x->consts, a, s));
+        AQ_CUDA(launch_gather<2>(x->fast, x->consts, a, s));
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[2], s, cudaEventRecordExternal));
     if (x->dims == 3)
-        AQ_CUDA(launch_sweep<3>(x->consts, a, s));
+        AQ_CUDA(launch_sweep<3>(x->fast, x->consts, a, x->sweep_grid, s));
     else
-        AQ_CUDA(launch_sweep<2>(x->consts, a, s));
+        AQ_CUDA(launch_sweep<2>(x->fast, x->consts, a, x->sweep_grid, s));
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[3], s, cudaEventRecordExternal));
     AQ_CUDA(launch_finalize(x->sc, s));
@@ -328,10 +331,15 @@ aqua_create(const aqua_params* params, uint32_t capacity,
         return AQUA_ERR_INVALID;
     }
     x->passes = sort_passes(bits_for(x->ncap));
-    if (cudaGetDevice(&x->device) != cudaSuccess) {
+    int sms = 0;
+    if (cudaGetDevice(&x->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount,
+                               x->device) != cudaSuccess) {
         delete x;
         return AQUA_ERR_CUDA;
     }
+    // persistent sweep: up to 8 resident blocks per SM fetch chunks
+    x->sweep_grid = (unsigned)(sms > 0 ? sms : 1) * 8u;
     x->pool_bytes = layout(x, nullptr);
     if (cudaMalloc(&x->pool, x->pool_bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -391,6 +399,16 @@ aqua_set_extras(aqua_ctx* x, int on)
     if (!x)
         return AQUA_ERR_INVALID;
     x->extras = on ? 1 : 0;
+    drop_graphs(x);
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_set_precision(aqua_ctx* x, int mode)
+{
+    if (!x || (mode != AQUA_PRECISION_EXACT && mode != AQUA_PRECISION_FAST))
+        return AQUA_ERR_INVALID;
+    x->fast = (mode == AQUA_PRECISION_FAST) ? 1 : 0;
     drop_graphs(x);
     return AQUA_OK;
 }
@@ -475,10 +493,7 @@ aqua_get_extra(aqua_ctx* x, aqua_extra* e, int on_host, void* stream)
     AQ_TRY(copy_out(e->id_unsorted, b.vals[x->passes & 1], N * 4, on_host, s));
     AQ_TRY(copy_out(e->id_sorted, b.id_sorted, N * 4, on_host, s));
     if (e->ihoc) {
-        if (x->dims == 3)
-            AQ_CUDA(launch_export_ihoc<3>(b.cells, x->ihoc_out, x->ncap, x->sc, s));
-        else
-            AQ_CUDA(launch_export_ihoc<2>(b.cells, x->ihoc_out, x->ncap, x->sc, s));
+        AQ_CUDA(launch_export_ihoc(b.cells, x->ihoc_out, x->ncap, x->sc, s));
         AQ_TRY(copy_out(e->ihoc, x->ihoc_out, (size_t)x->ncap * 4, on_host, s));
     }
     AQ_TRY(copy_out(e->grad_p, b.grad_p, N * VS * 4, on_host, s));
@@ -665,8 +680,8 @@ aqua_launches_per_step(aqua_ctx* x)
     if (!x)
         return 0;
     // begin, minmax, icell+hist, (passes - 1) hist, passes x (scan, scatter),
-    // gather, sweep, finalize
-    return 3u + (x->passes - 1u) + 2u * x->passes + 3u;
+    // gather, chunks, sweep, finalize
+    return 3u + (x->passes - 1u) + 2u * x->passes + 4u;
 }
 
 }  // extern "C"

@@ -55,8 +55,10 @@ struct DevScalars
     float dt;          // time step of the step being run
     uint32_t dt_next;  // bits of the running minimum of dt_var (atomicMin)
     uint32_t iter;
-    uint32_t err;      // error bits
-    uint32_t pad[3];
+    uint32_t err;         // error bits
+    uint32_t n_chunks;    // cell-aligned sweep chunks of this step
+    uint32_t chunk_next;  // next chunk to hand out (work counter)
+    uint32_t pad;
 };
 
 // One set of the per-particle Variables (reference layout)
@@ -86,6 +88,7 @@ struct StepBufs
     uint32_t* counts;      // per-pass digit x block counts
     uint32_t* digit_total; // per-pass digit totals (256)
     uint2* cells;          // (start, end) per cell; (N, N) if empty
+    uint2* chunks;         // (first, count) sweep chunks (<= N)
     uint8_t* cell_wall;    // 1 if the cell holds a boundary element
     uint32_t* id_sorted;   // old -> new
     // sorted start-of-step Variables (the reference's *_in after the

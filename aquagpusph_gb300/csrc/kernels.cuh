@@ -8,6 +8,7 @@ namespace aqua {
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
+constexpr int kSweepThreads = 128;
 
 // The reference's vec type: float4 in 3-D, float2 in 2-D
 template<int D>
@@ -84,14 +85,32 @@ struct StepArgs
     DevScalars* sc;
     int extras;        // write the intermediate operators
 };
+// gather / sweep of the step in the exact (IEEE, no FMA) or fast
+// (-use_fast_math) compilation
 template<int D>
-cudaError_t launch_gather(const Consts& c, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_gather(bool fast, const Consts& c, const StepArgs& a,
+                          cudaStream_t s);
 template<int D>
-cudaError_t launch_sweep(const Consts& c, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_sweep(bool fast, const Consts& c, const StepArgs& a,
+                         unsigned grid, cudaStream_t s);
 cudaError_t launch_finalize(DevScalars* sc, cudaStream_t s);
-template<int D>
 cudaError_t launch_export_ihoc(const uint2* cells, uint32_t* ihoc,
                                uint32_t ncap, const DevScalars* sc,
                                cudaStream_t s);
+
+namespace exact {
+template<int D>
+cudaError_t launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
+template<int D>
+cudaError_t launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
+                              cudaStream_t s);
+}  // namespace exact
+namespace fast {
+template<int D>
+cudaError_t launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
+template<int D>
+cudaError_t launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
+                              cudaStream_t s);
+}  // namespace fast
 
 }  // namespace aqua

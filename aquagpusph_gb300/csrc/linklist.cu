@@ -95,6 +95,8 @@ k_begin(DevScalars* sc, uint2* cells, uint8_t* cell_wall, uint32_t ncap,
             sc->r_max[k] = -INFINITY;
         }
         sc->dt_next = __float_as_uint(INFINITY);
+        sc->n_chunks = 0;
+        sc->chunk_next = 0;
     }
     if (sc->err)
         return;

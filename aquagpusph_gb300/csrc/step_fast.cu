@@ -1,0 +1,12 @@
+// The step kernels compiled with -use_fast_math (FMA contraction,
+// approximate division and square root): aqua::fast.  Same source as the
+// exact kernels (step_kernels.cuh); results stay within the 1e-5 relative
+// tolerance of the reference's per-step rates (tests/test_gpu_fast.py).
+#include "aqua_internal.cuh"
+#include "kernels.cuh"
+
+namespace aqua {
+namespace fast {
+#include "step_kernels.cuh"
+}  // namespace fast
+}  // namespace aqua

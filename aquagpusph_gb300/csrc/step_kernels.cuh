@@ -1,0 +1,607 @@
+// Kernel templates of one canonical WCSPH step: the sorted gather and the
+// fused neighbour sweep.  This file is compiled twice, into the namespaces
+// aqua::exact (step.cu: -fmad=false, IEEE division and square root -- the
+// reference's arithmetic, bit-exact with the CPU oracle) and aqua::fast
+// (step_fast.cu: -use_fast_math -- FMA contraction and approximate
+// division/square root, within the 1e-5 relative tolerance of the
+// reference's rates).
+//
+// The reference runs ~20 kernels and copies per step (basic.xml:132-171 and
+// the midpoint/domain/cfd/deltaSPH/BIe/variableTimeStep presets).  Here:
+//
+//   k_gather  = predictor backups + Domain + sort stage1/stage2 + EOS +
+//               Binormal + midpoint init copies + midpoint advance +
+//               midpoint EOS (one pass over the sorted order; it also writes
+//               the cell table and packs the neighbour data)
+//   k_sweep   = cfd Shepard + cfd interactions + cfd sensors + sensors
+//               renormalization + cfd lap p + BIe interactions, in ONE
+//               traversal of the 3^D neighbour cells, then per particle:
+//               BIe rates + cfd rates + delta-SPH + BIe elastic bounce +
+//               midpoint relax + corrector + BIe pst + variable time step
+//               + block min of dt_var (grid minimum by atomicMin)
+//
+// Every accumulator visits its neighbours in the reference order (27 cells,
+// x offset outermost; particles of a cell in sorted order) and each
+// expression keeps the reference's evaluation order.
+//
+// Work distribution of the sweep: a warp takes a chunk of <= 32 particles
+// of ONE cell (chunks are built by k_chunks, fetched dynamically), so all
+// lanes walk the same 27 neighbour cells and every neighbour load is a
+// warp-wide broadcast.
+//
+// Reference kernels (resources/Scripts/...): basic/time_scheme/midpoint.cl,
+// basic/Domain.cl, basic/Sort.cl, basic/EOS.cl, basic/Binormal.cl,
+// basic/Shepard.cl, cfd/Interactions.cl, cfd/Sensors.cl,
+// cfd/SensorsRenormalization.cl, basic/deltaSPH.cl (lapp, deltaSPH),
+// cfd/Boundary/BIe/{Interactions,Rates,ElasticBounce,PST}.cl, cfd/Rates.cl,
+// cfd/TimeStep.cl, KernelFunctions/Wendland{2D,3D}.hcl.
+//
+// This header has no include guard: it is meant to be included once per
+// namespace by step.cu and step_fast.cu.
+
+namespace {
+
+// Wendland C2 (Wendland{2D,3D}.hcl:44-66); the constants are float
+// products folded at compile time, as the OpenCL compiler folds them
+template<int D>
+struct WendlandC;
+template<>
+struct WendlandC<3>
+{
+    static constexpr float W = 0.08203125f * 0.318309886f;
+    static constexpr float F = 0.8203125f * 0.318309886f;
+};
+template<>
+struct WendlandC<2>
+{
+    static constexpr float W = 0.109375f * 0.318309886f;
+    static constexpr float F = 1.09375f * 0.318309886f;
+};
+
+template<int D>
+__device__ __forceinline__ float
+kernel_w(float q)
+{
+    const float a = 2.f - q;
+    float w = WendlandC<D>::W * (1.f + 2.f * q);
+    w = w * a;
+    w = w * a;
+    w = w * a;
+    return w * a;
+}
+
+template<int D>
+__device__ __forceinline__ float
+kernel_f(float q)
+{
+    const float a = 2.f - q;
+    float f = WendlandC<D>::F * a;
+    f = f * a;
+    return f * a;
+}
+
+__device__ __forceinline__ float
+cl_min(float x, float y)
+{
+    return (y < x) ? y : x;
+}
+__device__ __forceinline__ float
+cl_max(float x, float y)
+{
+    return (x < y) ? y : x;
+}
+
+template<int D>
+__device__ __forceinline__ float
+dot_d(const float* a, const float* b)
+{
+    float s = a[0] * b[0];
+    s = s + a[1] * b[1];
+    if (D == 3)
+        s = s + a[2] * b[2];
+    return s;
+}
+
+// dot over the storage vector (float4 in 3-D, including w)
+template<int D>
+__device__ __forceinline__ float
+dot_full(const float* a, const float* b)
+{
+    float s = a[0] * b[0];
+    s = s + a[1] * b[1];
+    if (D == 3) {
+        s = s + a[2] * b[2];
+        s = s + a[3] * b[3];
+    }
+    return s;
+}
+
+// Neighbour cell k (0 .. 3^D-1) of cell c in the reference order: x offset
+// outermost, then y, then z
+template<int D>
+__device__ __forceinline__ uint32_t
+neighbour_cell(uint32_t c, int k, uint32_t nx, uint32_t nxy)
+{
+    if (D == 3) {
+        const int ci = k / 9 - 1, cj = (k / 3) % 3 - 1, ck = k % 3 - 1;
+        return c + (uint32_t)ci + (uint32_t)cj * nx + (uint32_t)ck * nxy;
+    } else {
+        const int ci = k / 3 - 1, cj = k % 3 - 1;
+        return c + (uint32_t)ci + (uint32_t)cj * nx;
+    }
+}
+
+template<int D>
+__device__ __forceinline__ void
+load_normal(const float* normal, uint32_t j, float n[3])
+{
+    if (D == 3) {
+        const float4 v = reinterpret_cast<const float4*>(normal)[j];
+        n[0] = v.x;
+        n[1] = v.y;
+        n[2] = v.z;
+    } else {
+        const float2 v = reinterpret_cast<const float2*>(normal)[j];
+        n[0] = v.x;
+        n[1] = v.y;
+        n[2] = 0.f;
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ gather
+
+template<int D>
+__global__ void __launch_bounds__(256)
+k_gather(Consts c, StepArgs a)
+{
+    constexpr int VS = Vec<D>::VS;
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.N || a.sc->err)
+        return;
+    const uint32_t N = a.N;
+    const uint32_t key = a.skeys[s];
+    if (key >= a.ncap) {
+        atomicOr(&a.sc->err, kErrCapacity);
+        return;
+    }
+    const uint32_t o = a.perm[s];
+    a.b.id_sorted[o] = s;
+    if (s == 0 || a.skeys[s - 1] != key)
+        a.b.cells[key].x = s;
+    if (s == N - 1 || a.skeys[s + 1] != key)
+        a.b.cells[key].y = s + 1;
+
+    const VarSet& S = a.src;
+    const VarSet& T = a.dst;
+    const float dt = a.sc->dt;
+    const float hdt = 0.5f * dt;
+
+    // Domain (on the predictor backups) + sort stage1
+    int im = S.imove[o];
+    float r[4] = { 0.f, 0.f, 0.f, 0.f };
+    Vec<D>::load(S.r, o, r);
+    bool removed = false;
+    if (im > -255) {
+        bool out = false;
+        for (int k = 0; k < D; k++)
+            out = out || isnan(r[k]) || isinf(r[k]) || r[k] < c.domain_min[k] ||
+                  r[k] > c.domain_max[k];
+        if (out) {
+            removed = true;
+            im = -256;
+            for (int k = 0; k < VS; k++)
+                r[k] = c.domain_max[k];
+        }
+    }
+    const uint32_t set_raw = S.iset[o];
+    // out-of-range sets read set 0 (the per-set arrays hold n_sets entries)
+    const uint32_t set = set_raw < c.n_sets ? set_raw : 0u;
+    T.id[s] = S.id[o];
+    T.iset[s] = set_raw;
+    T.imove[s] = im;
+    float nrm[4], tng[4], bn[4] = { 0.f, 0.f, 0.f, 0.f };
+    Vec<D>::load(S.normal, o, nrm);
+    Vec<D>::load(S.tangent, o, tng);
+    // Binormal.cl
+    if (D == 3) {
+        bn[0] = nrm[1] * tng[2] - nrm[2] * tng[1];
+        bn[1] = nrm[2] * tng[0] - nrm[0] * tng[2];
+        bn[2] = nrm[0] * tng[1] - nrm[1] * tng[0];
+        bn[3] = 0.f;
+    } else {
+        tng[0] = nrm[1];
+        tng[1] = -nrm[0];
+    }
+    Vec<D>::store(T.normal, s, nrm);
+    Vec<D>::store(T.tangent, s, tng);
+    Vec<D>::store(T.binormal, s, bn);
+
+    // sort stage2 (+ Domain zeroing of u_in and m)
+    const float m = removed ? 0.f : S.m[o];
+    float uin[4] = { 0.f, 0.f, 0.f, 0.f }, ain[4] = { 0.f, 0.f, 0.f, 0.f };
+    if (!removed)
+        Vec<D>::load(S.u, o, uin);
+    Vec<D>::load(S.dudt, o, ain);
+    const float rho_in = S.rho[o];
+    const float drhodt_in = S.drhodt[o];
+
+    // midpoint advance (imove > 0), midpoint EOS
+    float uh[4];
+    float rho_h = rho_in;
+    for (int k = 0; k < 4; k++)
+        uh[k] = uin[k];
+    if (im > 0) {
+        for (int k = 0; k < VS; k++)
+            uh[k] = uin[k] + hdt * ain[k];
+        rho_h = rho_in + hdt * drhodt_in;
+    }
+    float p;
+    if (im > 0 || im == -1)
+        p = c.p0 + c.cs * c.cs * (rho_h - c.refd[set]);
+    else
+        p = S.p[s];  // the pressure Variable is not permuted by the sort
+
+    Vec<D>::store(T.r, s, r);
+    Vec<D>::store(a.b.r_in, s, r);
+    Vec<D>::store(T.u, s, uh);
+    Vec<D>::store(a.b.u_in, s, uin);
+    Vec<D>::store(T.dudt, s, ain);
+    Vec<D>::store(a.b.dudt_in, s, ain);
+    T.rho[s] = rho_h;
+    a.b.rho_in[s] = rho_in;
+    T.drhodt[s] = drhodt_in;
+    a.b.drhodt_in[s] = drhodt_in;
+    T.m[s] = m;
+    T.p[s] = p;
+    a.b.posq[s] = make_float4(r[0], r[1], D == 3 ? r[2] : 0.f, __int_as_float(im));
+    a.b.velq[s] = make_float4(uh[0], uh[1], D == 3 ? uh[2] : 0.f, rho_h);
+    a.b.pmq[s] = make_float2(p, m);
+    if (im == -3)
+        a.b.cell_wall[key] = 1;
+}
+
+// ------------------------------------------------------------------- sweep
+
+// Everything the sweep does for sorted particle i; returns its dt_var (or
+// +inf when the particle has none)
+template<int D>
+__device__ __forceinline__ float
+sweep_particle(const Consts& c, const StepArgs& a, uint32_t i)
+{
+    constexpr int VS = Vec<D>::VS;
+    constexpr int NC = (D == 3) ? 27 : 9;
+    const float dt = a.sc->dt;
+    const float hdt = 0.5f * dt;
+    const float4 pi = a.b.posq[i];
+    const int im = __float_as_int(pi.w);
+    const VarSet& T = a.dst;
+    const uint32_t nx = a.sc->n_cells[0];
+    const uint32_t nxy = a.sc->n_cells[0] * a.sc->n_cells[1];
+    const uint32_t key_i = a.skeys[i];
+    const bool fluid = (im == 1), sensor = (im == 0);
+    const bool want_shep = (im >= -3) && (im <= 1);
+
+    float shep = 0.f;
+    float gp[3] = { 0.f, 0.f, 0.f }, lu[3] = { 0.f, 0.f, 0.f };
+    float gw[3] = { 0.f, 0.f, 0.f };
+    float du = 0.f, lp = 0.f, dbi = 0.f;
+    float su[3] = { 0.f, 0.f, 0.f }, sr = 0.f, sp = 0.f;
+    float ui_full[4];
+    Vec<D>::load(T.u, i, ui_full);  // half-step velocity incl. w
+    const float4 vi = a.b.velq[i];
+    const float rho_i = vi.w;
+    const float p_i = a.b.pmq[i].x;
+    const float ri[3] = { pi.x, pi.y, pi.z };
+    const float uiv[3] = { vi.x, vi.y, vi.z };
+
+    if (want_shep) {
+        for (int k = 0; k < NC; k++) {
+            const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
+            const uint2 se = a.b.cells[cn];
+            for (uint32_t j = se.x; j < se.y; j++) {
+                const float4 pj = a.b.posq[j];
+                const int jm = __float_as_int(pj.w);
+                if (jm != 1 && !(fluid && jm == -3))
+                    continue;
+                float d[3];
+                d[0] = pj.x - ri[0];
+                d[1] = pj.y - ri[1];
+                d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
+                const float rr = dot_d<D>(d, d);
+                if (rr >= c.q2_reject)
+                    continue;
+                const float q = sqrtf(rr) / c.H;
+                if (q >= c.SUPPORT)
+                    continue;
+                if (jm == 1) {
+                    const float4 vj = a.b.velq[j];
+                    const float2 pmj = a.b.pmq[j];
+                    const float rho_j = vj.w, m_j = pmj.y;
+                    const float wj = kernel_w<D>(q) * c.CONW * m_j / rho_j;
+                    shep = shep + wj;
+                    if (j == i)
+                        continue;
+                    if (fluid) {
+                        const float p_j = pmj.x;
+                        float dv[3];
+                        dv[0] = vj.x - uiv[0];
+                        dv[1] = vj.y - uiv[1];
+                        dv[2] = (D == 3) ? vj.z - uiv[2] : 0.f;
+                        const float udr = dot_d<D>(dv, d);
+                        const float f_ij = kernel_f<D>(q) * c.CONF * m_j;
+                        const float rr_ij = rho_i * rho_j;
+                        const float sgp = (p_i + p_j) / rr_ij * f_ij;
+                        const float slu = f_ij * 2.f / rr_ij;
+                        for (int kk = 0; kk < D; kk++) {
+                            gp[kk] = gp[kk] + sgp * d[kk];
+                            lu[kk] = lu[kk] + slu * dv[kk];
+                        }
+                        du = du + udr * f_ij * rho_i / rho_j;
+                        lp = lp + (p_j - p_i) * (f_ij / rho_j);
+                    } else if (sensor) {
+                        su[0] = su[0] + vj.x * wj;
+                        su[1] = su[1] + vj.y * wj;
+                        if (D == 3)
+                            su[2] = su[2] + vj.z * wj;
+                        sr = sr + rho_j * wj;
+                        sp = sp + pmj.x * wj;
+                    }
+                } else {
+                    // boundary element: BIe wall sums (fluid i only)
+                    float nj[3];
+                    load_normal<D>(a.dst.normal, j, nj);
+                    const float4 vj = a.b.velq[j];
+                    const float uj[3] = { vj.x, vj.y, vj.z };
+                    const float wa = kernel_w<D>(q) * c.CONW * a.b.pmq[j].y;
+                    float g[3];
+                    for (int kk = 0; kk < D; kk++) {
+                        g[kk] = nj[kk] * wa;
+                        gw[kk] = gw[kk] + g[kk];
+                    }
+                    dbi = dbi - dot_d<D>(uj, g);
+                }
+            }
+        }
+    }
+    if (a.b.shepard)
+        a.b.shepard[i] = want_shep ? shep : 0.f;
+
+    float gpf[4] = { 0.f, 0.f, 0.f, 0.f }, luf[4] = { 0.f, 0.f, 0.f, 0.f };
+    float gwf[4] = { 0.f, 0.f, 0.f, 0.f };
+    float div_u = 0.f;
+    if (fluid) {
+        for (int k = 0; k < D; k++) {
+            gpf[k] = gp[k];
+            luf[k] = lu[k];
+            gwf[k] = gw[k];
+        }
+        // BIe Rates.cl
+        const float s2 = 2.f * p_i / rho_i;
+        for (int k = 0; k < VS; k++)
+            gpf[k] = gpf[k] + s2 * gwf[k];
+        div_u = du - 2.f * rho_i * (dot_full<D>(ui_full, gwf) + dbi);
+    }
+    if (a.extras) {
+        Vec<D>::store(a.b.grad_p, i, gpf);
+        Vec<D>::store(a.b.lap_u, i, luf);
+        Vec<D>::store(a.b.grad_w_bi, i, gwf);
+        a.b.div_u[i] = div_u;
+        a.b.lap_p[i] = fluid ? lp : 0.f;
+        a.b.div_u_bi[i] = fluid ? dbi : 0.f;
+    }
+
+    if (sensor) {
+        float shp = shep;
+        if (shp < 1.0e-6f)
+            shp = 1.f;
+        float uo[4];
+        for (int k = 0; k < 4; k++)
+            uo[k] = ui_full[k];
+        for (int k = 0; k < D; k++)
+            uo[k] = su[k];
+        for (int k = 0; k < VS; k++)
+            uo[k] = uo[k] / shp;
+        Vec<D>::store(T.u, i, uo);
+        T.rho[i] = sr / shp;
+        T.p[i] = sp / shp;
+    }
+
+    if (im <= 0)
+        return c.dt_fixed;
+
+    const uint32_t set_raw = T.iset[i];
+    const uint32_t set = set_raw < c.n_sets ? set_raw : 0u;
+    float acc[4];
+    float drhodt;
+    float ain[4];
+    Vec<D>::load(a.b.dudt_in, i, ain);
+    const float drhodt_in = a.b.drhodt_in[i];
+    float uin[4] = { 0.f, 0.f, 0.f, 0.f };
+    Vec<D>::load(a.b.u_in, i, uin);
+    if (fluid) {
+        // cfd Rates.cl + deltaSPH
+        const float visc = c.visc_dyn[set];
+        for (int k = 0; k < VS; k++)
+            acc[k] = -gpf[k] + visc * luf[k] + c.g[k];
+        drhodt = -div_u;
+        const float delta_f = c.delta[set] * dt * rho_i / c.refd[set];
+        drhodt = drhodt + delta_f * lp;
+        // BIe ElasticBounce.cl
+        if (dt != 0.f) {
+            float vh[3];
+            for (int k = 0; k < D; k++)
+                vh[k] = uin[k] + hdt * acc[k];
+            for (int k = 0; k < NC; k++) {
+                const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
+                if (!a.b.cell_wall[cn])
+                    continue;
+                const uint2 se = a.b.cells[cn];
+                for (uint32_t j = se.x; j < se.y; j++) {
+                    const float4 pj = a.b.posq[j];
+                    if (__float_as_int(pj.w) != -3)
+                        continue;
+                    float d[3], nj[3], t[3];
+                    d[0] = pj.x - ri[0];
+                    d[1] = pj.y - ri[1];
+                    d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
+                    load_normal<D>(a.dst.normal, j, nj);
+                    const float rn = dot_d<D>(d, nj);
+                    if (rn < 0.f)
+                        continue;
+                    const float mj = a.b.pmq[j].y;
+                    const float dr = (D == 3) ? sqrtf(mj) : mj;
+                    const float R = c.dr_factor * dr;
+                    for (int kk = 0; kk < D; kk++)
+                        t[kk] = d[kk] - rn * nj[kk];
+                    if (dot_d<D>(t, t) >= R * R)
+                        continue;
+                    const float drn = dt * dot_d<D>(vh, nj);
+                    if (drn < 0.f)
+                        continue;
+                    if (rn - drn <= c.min_bound_dist * dr) {
+                        float v[3], vr[3];
+                        for (int kk = 0; kk < D; kk++)
+                            v[kk] = uin[kk] + dt * acc[kk];
+                        const float vn2 = 2.f * dot_d<D>(v, nj);
+                        for (int kk = 0; kk < D; kk++)
+                            vr[kk] = v[kk] - vn2 * nj[kk];
+                        for (int kk = 0; kk < D; kk++) {
+                            acc[kk] = (vr[kk] - uin[kk]) / dt;
+                            vh[kk] = uin[kk] + hdt * acc[kk];
+                        }
+                    }
+                }
+            }
+        }
+    } else {
+        for (int k = 0; k < VS; k++)
+            acc[k] = ain[k];
+        drhodt = drhodt_in;
+    }
+    // midpoint relax
+    const float rl = c.relax_midpoint;
+    for (int k = 0; k < VS; k++)
+        acc[k] = rl * ain[k] + (1.f - rl) * acc[k];
+    drhodt = rl * drhodt_in + (1.f - rl) * drhodt;
+    // corrector
+    float rin[4] = { 0.f, 0.f, 0.f, 0.f };
+    Vec<D>::load(a.b.r_in, i, rin);
+    const float hdt2 = 0.5f * dt * dt;
+    float rn_[4] = { 0.f, 0.f, 0.f, 0.f }, un[4] = { 0.f, 0.f, 0.f, 0.f };
+    for (int k = 0; k < VS; k++) {
+        rn_[k] = rin[k] + dt * uin[k] + hdt2 * acc[k];
+        un[k] = uin[k] + dt * acc[k];
+    }
+    const float rho_n = a.b.rho_in[i] + dt * drhodt;
+    // BIe PST.cl
+    if (fluid) {
+        const float Ri = 0.5f * powf(T.m[i] / rho_n, 1.f / c.DIMS);
+        for (int k = 0; k < NC; k++) {
+            const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
+            if (!a.b.cell_wall[cn])
+                continue;
+            const uint2 se = a.b.cells[cn];
+            for (uint32_t j = se.x; j < se.y; j++) {
+                const float4 pj = a.b.posq[j];
+                if (__float_as_int(pj.w) != -3)
+                    continue;
+                float d[3], nj[3], t[3];
+                d[0] = pj.x - rn_[0];
+                d[1] = pj.y - rn_[1];
+                d[2] = (D == 3) ? pj.z - rn_[2] : 0.f;
+                load_normal<D>(a.dst.normal, j, nj);
+                const float rn = dot_d<D>(d, nj);
+                if (fabsf(rn) > Ri)
+                    continue;
+                const float mj = a.b.pmq[j].y;
+                const float dr = (D == 3) ? sqrtf(mj) : mj;
+                const float Rj = c.dr_factor * dr;
+                for (int kk = 0; kk < D; kk++)
+                    t[kk] = d[kk] - rn * nj[kk];
+                if (dot_d<D>(t, t) >= Rj * Rj)
+                    continue;
+                const float sh = rn - Ri;
+                for (int kk = 0; kk < D; kk++)
+                    rn_[kk] = rn_[kk] + sh * nj[kk];
+            }
+        }
+    }
+    Vec<D>::store(T.dudt, i, acc);
+    T.drhodt[i] = drhodt;
+    Vec<D>::store(T.r, i, rn_);
+    Vec<D>::store(T.u, i, un);
+    T.rho[i] = rho_n;
+    // TimeStep.cl
+    const float dr_max = c.dt_Ma * c.h;
+    const float dt_u = c.courant * dr_max / sqrtf(dot_full<D>(un, un));
+    return cl_max(cl_min(c.dt_fixed, dt_u), c.dt_min);
+}
+
+// Persistent sweep: warps fetch cell-aligned chunks of <= 32 particles
+template<int D>
+__global__ void __launch_bounds__(kSweepThreads, 6)
+k_sweep(Consts c, StepArgs a)
+{
+    __shared__ float s_dtmin[kSweepThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float dt_min = INFINITY;
+    if (a.sc->err == 0) {
+        const uint32_t nch = a.sc->n_chunks;
+        for (;;) {
+            uint32_t ch = 0;
+            if (lane == 0)
+                ch = atomicAdd(&a.sc->chunk_next, 1u);
+            ch = __shfl_sync(0xffffffffu, ch, 0);
+            if (ch >= nch)
+                break;
+            const uint2 cw = a.b.chunks[ch];
+            if ((uint32_t)lane < cw.y)
+                dt_min = cl_min(dt_min, sweep_particle<D>(c, a, cw.x + lane));
+        }
+    }
+    // block minimum of dt_var, one atomic per block
+    for (int o = 16; o > 0; o >>= 1)
+        dt_min = cl_min(dt_min, __shfl_xor_sync(0xffffffffu, dt_min, o));
+    if (lane == 0)
+        s_dtmin[warp] = dt_min;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = s_dtmin[0];
+        for (int w = 1; w < kSweepThreads / 32; w++)
+            m = cl_min(m, s_dtmin[w]);
+        if (m < INFINITY && m >= 0.f)
+            atomicMin(&a.sc->dt_next, __float_as_uint(m));
+        else if (!(m >= 0.f))
+            atomicOr(&a.sc->err, kErrDt);
+    }
+}
+
+template<int D>
+cudaError_t
+launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s)
+{
+    if (a.N == 0)
+        return cudaSuccess;
+    k_gather<D><<<(a.N + 255) / 256, 256, 0, s>>>(c, a);
+    return cudaGetLastError();
+}
+
+template<int D>
+cudaError_t
+launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
+                  cudaStream_t s)
+{
+    if (a.N == 0)
+        return cudaSuccess;
+    k_sweep<D><<<grid, kSweepThreads, 0, s>>>(c, a);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_gather_impl<2>(const Consts&, const StepArgs&, cudaStream_t);
+template cudaError_t launch_gather_impl<3>(const Consts&, const StepArgs&, cudaStream_t);
+template cudaError_t launch_sweep_impl<2>(const Consts&, const StepArgs&, unsigned,
+                                          cudaStream_t);
+template cudaError_t launch_sweep_impl<3>(const Consts&, const StepArgs&, unsigned,
+                                          cudaStream_t);

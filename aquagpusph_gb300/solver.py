@@ -56,6 +56,12 @@ class Solver:
     def set_extras(self, on: bool = True):
         _lib.check("aqua_set_extras", self.lib.aqua_set_extras(self.ctx, int(on)))
 
+    def set_precision(self, fast: bool):
+        """Exact (reference arithmetic, default) or fast step kernels."""
+        mode = _lib.AQUA_PRECISION_FAST if fast else _lib.AQUA_PRECISION_EXACT
+        _lib.check("aqua_set_precision",
+                   self.lib.aqua_set_precision(self.ctx, mode))
+
     def set_params(self, params: Params):
         self.params = params
         self._pstruct, self._pkeep = _lib.params_struct(params)

@@ -224,6 +224,7 @@ def run_ours(args):
     c, desc = workload(args.workload)
     three_d = c.dims == 3
     sv = Solver(c.params, capacity=c.N)
+    sv.set_precision(args.precision == "fast")
     sv.set_case(c)
     stream = torch.cuda.Stream()
     sid = stream.cuda_stream
@@ -377,6 +378,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c1s", "c1m"])
     ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--precision", default="exact", choices=["exact", "fast"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

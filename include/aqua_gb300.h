@@ -158,6 +158,17 @@ aqua_status aqua_set_params(aqua_ctx* ctx, const aqua_params* params);
  * need them). */
 aqua_status aqua_set_extras(aqua_ctx* ctx, int on);
 
+/* Arithmetic of the step kernels.  AQUA_PRECISION_EXACT (the default):
+ * every operation of the reference's kernels as one correctly rounded IEEE
+ * binary32 operation in the reference's order, no FMA contraction -- the
+ * results equal the reference kernels' bit for bit (positions up to the
+ * last bit of powf in the BIe PST).  AQUA_PRECISION_FAST: the same kernels
+ * compiled with FMA contraction and approximate division / square root;
+ * per-step rates stay within 1e-5 relative of the exact ones. */
+#define AQUA_PRECISION_EXACT 0
+#define AQUA_PRECISION_FAST 1
+aqua_status aqua_set_precision(aqua_ctx* ctx, int mode);
+
 /* Uploads the particle Variables of an N-particle case into the resident
  * state (the ParticlesSet loaders, FileManager.cpp:136-139).  `on_host` = 1
  * for host pointers (pinned memory makes the copies asynchronous), 0 for
