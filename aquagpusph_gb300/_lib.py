@@ -24,6 +24,7 @@ AQUA_ERR_NONFINITE = -6
 
 AQUA_PRECISION_EXACT = 0
 AQUA_PRECISION_FAST = 1
+AQUA_NOALLOC_SORT_MAX_KEYS = 1 << 20
 
 STATUS_NAMES = {
     AQUA_OK: "AQUA_OK",
@@ -113,6 +114,8 @@ SIGNATURES = [
     ("aqua_radix_sort", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_uint32, C.c_uint32,
                                   C.c_void_p]),
+    ("aqua_radix_sort_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_uint32, C.c_uint32, C.c_void_p]),
     ("aqua_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("aqua_stage_times", C.c_int, [C.c_void_p, _F, C.c_uint32]),
     ("aqua_launches_per_step", C.c_uint32, [C.c_void_p]),

@@ -229,6 +229,21 @@ aqua_status aqua_radix_sort(aqua_ctx* ctx, uint32_t* keys, uint32_t* perm,
 aqua_status aqua_set_profiling(aqua_ctx* ctx, int on);
 aqua_status aqua_stage_times(aqua_ctx* ctx, float* ms, uint32_t n);
 
+/* The stable radix sort of aqua_radix_sort(), for callers that cannot
+ * allocate device memory: no context, no cudaMalloc, no allocating library
+ * call.  It has no counterpart in the reference.  Its scratch is a
+ * fixed-size array of the library (about 12.6 MB, present on every GPU that
+ * loads the library until the process exits), so n is limited to
+ * AQUA_NOALLOC_SORT_MAX_KEYS; larger n returns AQUA_ERR_CAPACITY.  keys are
+ * sorted in place (values below 2^key_bits), perm[s] = original index and
+ * inv_perm[orig] = s (either may be NULL).  All calls on a device share the
+ * scratch: calls that overlap on the GPU race.  The first call on a device
+ * looks the scratch address up; make it before any stream capture. */
+#define AQUA_NOALLOC_SORT_MAX_KEYS (1u << 20)
+aqua_status aqua_radix_sort_noalloc(uint32_t* keys, uint32_t* perm,
+                                    uint32_t* inv_perm, uint32_t n,
+                                    uint32_t key_bits, void* stream);
+
 /* Number of kernel launches one aqua_step() step issues (for accounting). */
 uint32_t aqua_launches_per_step(aqua_ctx* ctx);
 
