@@ -12,7 +12,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "../../include/aqua_gb300.h"
+#include "aqua_gb300.h"
 
 namespace aqua {
 

@@ -9,6 +9,7 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
 constexpr int kSweepThreads = 128;
+constexpr int kSweepQueue = 128;   // queued neighbours per thread (power of 2)
 
 // The reference's vec type: float4 in 3-D, float2 in 2-D
 template<int D>

@@ -265,10 +265,24 @@ k_gather(Consts c, StepArgs a)
 // ------------------------------------------------------------------- sweep
 
 // Everything the sweep does for sorted particle i; returns its dt_var (or
-// +inf when the particle has none)
+// +inf when the particle has none).  All 32 lanes of a warp call it for
+// particles of the same cell (`valid` is false for the lanes past the end of
+// the chunk), so the neighbour scan below is warp-uniform.
+//
+// The neighbour loop runs in two phases so that the expensive pair
+// arithmetic executes with full warps: the scan walks the candidates of the
+// 3^D cells in the reference order and appends the ones inside the support
+// to this lane's ring queue in shared memory (one column per thread); the
+// drain pops the queue in order and accumulates.  Every sum keeps the
+// reference's order.  A queue entry is 16 bits: the neighbour-cell slot k
+// (5 bits) and the candidate's offset in that cell (11 bits); `cstart`
+// holds the first sorted index of the 3^D neighbour cells of the warp's
+// cell.  The scan checks the queues every 32 candidates, where they have
+// room for at least 32 more, so a queue never overflows.
 template<int D>
 __device__ __forceinline__ float
-sweep_particle(const Consts& c, const StepArgs& a, uint32_t i)
+sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
+               uint16_t* queue, uint32_t* cstart)
 {
     constexpr int VS = Vec<D>::VS;
     constexpr int NC = (D == 3) ? 27 : 9;
@@ -280,8 +294,8 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i)
     const uint32_t nx = a.sc->n_cells[0];
     const uint32_t nxy = a.sc->n_cells[0] * a.sc->n_cells[1];
     const uint32_t key_i = a.skeys[i];
-    const bool fluid = (im == 1), sensor = (im == 0);
-    const bool want_shep = (im >= -3) && (im <= 1);
+    const bool fluid = valid && (im == 1), sensor = valid && (im == 0);
+    const bool want_shep = valid && (im >= -3) && (im <= 1);
 
     float shep = 0.f;
     float gp[3] = { 0.f, 0.f, 0.f }, lu[3] = { 0.f, 0.f, 0.f };
@@ -296,28 +310,40 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i)
     const float ri[3] = { pi.x, pi.y, pi.z };
     const float uiv[3] = { vi.x, vi.y, vi.z };
 
-    if (want_shep) {
-        for (int k = 0; k < NC; k++) {
-            const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
-            const uint2 se = a.b.cells[cn];
-            for (uint32_t j = se.x; j < se.y; j++) {
-                const float4 pj = a.b.posq[j];
-                const int jm = __float_as_int(pj.w);
-                if (jm != 1 && !(fluid && jm == -3))
-                    continue;
-                float d[3];
-                d[0] = pj.x - ri[0];
-                d[1] = pj.y - ri[1];
-                d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
-                const float rr = dot_d<D>(d, d);
-                if (rr >= c.q2_reject)
-                    continue;
-                const float q = sqrtf(rr) / c.H;
-                if (q >= c.SUPPORT)
-                    continue;
-                if (jm == 1) {
-                    const float4 vj = a.b.velq[j];
-                    const float2 pmj = a.b.pmq[j];
+    uint32_t qh = 0, qt = 0;  // ring queue head / tail
+    // The drain is software-pipelined: the records of the next queued
+    // neighbour are loaded while the current pair is computed.
+    auto drain = [&](uint32_t upto) {
+        if (qh >= upto)
+            return;
+        uint32_t jn;
+        float4 pn, vn;
+        float2 mn;
+        auto fetch = [&](uint32_t h) {
+            const uint32_t e = queue[(h & (kSweepQueue - 1)) * kSweepThreads];
+            jn = cstart[e >> 11] + (e & 2047u);
+            pn = a.b.posq[jn];
+            vn = a.b.velq[jn];
+            mn = a.b.pmq[jn];
+        };
+        fetch(qh);
+        for (; qh < upto; qh++) {
+            const uint32_t j = jn;
+            const float4 pj = pn;
+            const float4 vj = vn;
+            const float2 pmj = mn;
+            if (qh + 1 < upto)
+                fetch(qh + 1);
+            const int jm = __float_as_int(pj.w);
+            float d[3];
+            d[0] = pj.x - ri[0];
+            d[1] = pj.y - ri[1];
+            d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
+            const float rr = dot_d<D>(d, d);
+            const float q = sqrtf(rr) / c.H;
+            if (q >= c.SUPPORT)
+                continue;
+            if (jm == 1) {
                     const float rho_j = vj.w, m_j = pmj.y;
                     const float wj = kernel_w<D>(q) * c.CONW * m_j / rho_j;
                     shep = shep + wj;
@@ -352,9 +378,8 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i)
                     // boundary element: BIe wall sums (fluid i only)
                     float nj[3];
                     load_normal<D>(a.dst.normal, j, nj);
-                    const float4 vj = a.b.velq[j];
                     const float uj[3] = { vj.x, vj.y, vj.z };
-                    const float wa = kernel_w<D>(q) * c.CONW * a.b.pmq[j].y;
+                    const float wa = kernel_w<D>(q) * c.CONW * pmj.y;
                     float g[3];
                     for (int kk = 0; kk < D; kk++) {
                         g[kk] = nj[kk] * wa;
@@ -362,9 +387,70 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i)
                     }
                     dbi = dbi - dot_d<D>(uj, g);
                 }
+        }
+    };
+
+    // first sorted index of each neighbour cell (same for the whole warp)
+    const int lane = threadIdx.x & 31;
+    if (lane < NC)
+        cstart[lane] = a.b.cells[neighbour_cell<D>(key_i, lane, nx, nxy)].x;
+    __syncwarp();
+    for (int k = 0; k < NC; k++) {
+        const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
+        const uint2 se = a.b.cells[cn];
+        const uint32_t count = se.y - se.x;
+        if (count > 2048u) {
+            // the 11-bit offsets cannot address such a cell
+            if (lane == 0)
+                atomicOr(&a.sc->err, kErrCapacity);
+            continue;
+        }
+        for (uint32_t g = 0; g < count; g += 32) {
+            // warp-uniform checkpoint: make room for the next 32 candidates,
+            // first draining the entries every lane has (full warps)
+            if (__any_sync(0xffffffffu, qt - qh > kSweepQueue - 32)) {
+                const uint32_t fill = qt - qh;
+                const uint32_t common = __reduce_min_sync(
+                    0xffffffffu, want_shep ? fill : 0xffffffffu);
+                drain(qh + min(common, fill));
+                if (__any_sync(0xffffffffu, qt - qh > kSweepQueue - 32))
+                    drain(qt);
+            }
+            const uint32_t gend = min(g + 32u, count);
+            // four candidates per iteration, loads first
+            for (uint32_t o = g; o < gend; o += 4) {
+                float4 p4[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (o + u < gend)
+                        p4[u] = a.b.posq[se.x + o + u];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (o + u >= gend)
+                        break;
+                    const float4 pj = p4[u];
+                    const int jm = __float_as_int(pj.w);
+                    const float d0 = pj.x - ri[0], d1 = pj.y - ri[1];
+                    float rr = d0 * d0 + d1 * d1;
+                    if (D == 3) {
+                        const float d2 = pj.z - ri[2];
+                        rr = rr + d2 * d2;
+                    }
+                    const bool take = want_shep &&
+                                      (jm == 1 || (fluid && jm == -3)) &&
+                                      rr < c.q2_reject;
+                    if (take) {
+                        queue[(qt & (kSweepQueue - 1)) * kSweepThreads] =
+                            (uint16_t)(((uint32_t)k << 11) | (o + u));
+                        qt++;
+                    }
+                }
             }
         }
     }
+    drain(qt);
+    if (!valid)
+        return INFINITY;
     if (a.b.shepard)
         a.b.shepard[i] = want_shep ? shep : 0.f;
 
@@ -541,10 +627,12 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i)
 
 // Persistent sweep: warps fetch cell-aligned chunks of <= 32 particles
 template<int D>
-__global__ void __launch_bounds__(kSweepThreads, 6)
+__global__ void __launch_bounds__(kSweepThreads, 5)
 k_sweep(Consts c, StepArgs a)
 {
     __shared__ float s_dtmin[kSweepThreads / 32];
+    __shared__ uint16_t s_queue[kSweepQueue * kSweepThreads];
+    __shared__ uint32_t s_cstart[kSweepThreads / 32][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float dt_min = INFINITY;
     if (a.sc->err == 0) {
@@ -557,8 +645,12 @@ k_sweep(Consts c, StepArgs a)
             if (ch >= nch)
                 break;
             const uint2 cw = a.b.chunks[ch];
-            if ((uint32_t)lane < cw.y)
-                dt_min = cl_min(dt_min, sweep_particle<D>(c, a, cw.x + lane));
+            const bool valid = (uint32_t)lane < cw.y;
+            const float v = sweep_particle<D>(c, a, valid ? cw.x + lane : cw.x,
+                                              valid, s_queue + threadIdx.x,
+                                              s_cstart[warp]);
+            __syncwarp();  // s_cstart is rewritten for the next chunk
+            dt_min = cl_min(dt_min, v);
         }
     }
     // block minimum of dt_var, one atomic per block
