@@ -82,6 +82,13 @@ class AquaExtra(C.Structure):
     _fields_ = list(EXTRA_FIELDS)
 
 
+class AquaCase(C.Structure):
+    _fields_ = [("t", C.c_float), ("dt", C.c_float), ("iter", C.c_uint32),
+                ("roll_enabled", C.c_int32), ("roll_iset", C.c_uint32),
+                ("roll_amplitude", C.c_float), ("roll_angular_freq", C.c_float),
+                ("roll_center", C.c_float * 4)]
+
+
 class AquaScalars(C.Structure):
     _fields_ = [("t", C.c_float), ("dt", C.c_float), ("iter", C.c_uint32),
                 ("n_cells", C.c_uint32 * 4), ("r_min", C.c_float * 4),
@@ -102,6 +109,10 @@ SIGNATURES = [
                                  C.c_void_p]),
     ("aqua_get_state", C.c_int, [C.c_void_p, C.POINTER(AquaVars), C.c_int,
                                  C.c_void_p]),
+    ("aqua_set_cases", C.c_int, [C.c_void_p, C.c_uint32, _U,
+                                 C.POINTER(AquaCase), C.c_void_p]),
+    ("aqua_get_case_scalars", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32,
+                                        C.POINTER(AquaScalars), C.c_void_p]),
     ("aqua_get_extra", C.c_int, [C.c_void_p, C.POINTER(AquaExtra), C.c_int,
                                  C.c_void_p]),
     ("aqua_get_scalars", C.c_int, [C.c_void_p, C.POINTER(AquaScalars),

@@ -306,3 +306,113 @@ def dam_break_3d(dx: float = 0.005, tank=(3.22, 1.0, 1.0),
                     domain_min=(-margin, -margin, -margin, 0.0),
                     domain_max=(Lx + margin, Wy + margin, Hz + margin, 0.0))
     return _fill_case(params, parts)
+
+
+@dataclasses.dataclass
+class Motion:
+    """Prescribed roll of a case's boundary elements and probes (particles
+    of set ``iset`` that are not fluid) about the z axis through ``center``:
+    psi(t) = amplitude * sin(angular_freq * t)."""
+    amplitude: float          # rad
+    angular_freq: float       # rad/s
+    center: tuple = (0.0, 0.0, 0.0, 0.0)
+    iset: int = 1
+
+
+@dataclasses.dataclass
+class Batch:
+    """Independent cases packed into one concatenated particle set: case k
+    holds particles [offsets[k], offsets[k+1]) of ``case``."""
+    case: Case
+    offsets: np.ndarray
+    motions: list
+    cases: list
+
+    @property
+    def n_cases(self) -> int:
+        return len(self.offsets) - 1
+
+
+def pack(cases: list, motions: list = None) -> Batch:
+    """Concatenates cases that share their Params into one Batch."""
+    params = cases[0].params
+    n = sum(c.N for c in cases)
+    big = Case(params, n)
+    offsets = np.zeros(len(cases) + 1, np.uint32)
+    o = 0
+    for k, c in enumerate(cases):
+        for name in big.state_arrays():
+            getattr(big, name)[o:o + c.N] = getattr(c, name)
+        o += c.N
+        offsets[k + 1] = o
+    big.id[:] = np.arange(n, dtype=np.uint32)
+    big.t, big.dt, big.iter = cases[0].t, cases[0].dt, cases[0].iter
+    return Batch(big, offsets, list(motions or [None] * len(cases)), cases)
+
+
+def sloshing_tank_2d(fill: float, dx: float = 0.004, tank=(0.9, 0.5),
+                     c0: float = 25.0, probe_above: float = 0.05,
+                     refd: float = 998.0, nu: float = 1.0e-6,
+                     delta: float = 0.1, g: float = 9.81,
+                     hfac: float = 2.0) -> Case:
+    """One closed 2-D sloshing tank (BIe walls on its four sides) filled to
+    ``fill`` with water at hydrostatic density, and a pressure probe on the
+    left wall ``probe_above`` above the still-water level."""
+    W, Ht = tank
+    nx = int(round(W / dx))
+    ny = int(round(fill / dx))
+    hf = ny * dx
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    x = (i.ravel() + 0.5) * dx
+    y = (j.ravel() + 0.5) * dx
+    press = refd * g * (hf - y)
+    dens = refd + press / c0 ** 2
+    parts = [dict(r=np.stack([x, y], 1), rho=dens, m=dens * dx ** 2, p=press,
+                  imove=np.full(len(x), FLUID), iset=np.zeros(len(x)))]
+    NX, NY = int(round(W / dx)), int(round(Ht / dx))
+    s = (np.arange(NX) + 0.5) * dx
+    t = (np.arange(NY) + 0.5) * dx
+    walls = [(np.stack([s, np.zeros_like(s)], 1), (0.0, -1.0)),
+             (np.stack([s, np.full_like(s, NY * dx)], 1), (0.0, 1.0)),
+             (np.stack([np.zeros_like(t), t], 1), (-1.0, 0.0)),
+             (np.stack([np.full_like(t, NX * dx), t], 1), (1.0, 0.0))]
+    for pos, nrm in walls:
+        k = len(pos)
+        parts.append(dict(r=pos, normal=np.tile(nrm, (k, 1)),
+                          tangent=np.tile((nrm[1], -nrm[0]), (k, 1)),
+                          rho=np.full(k, refd), m=np.full(k, dx), p=np.zeros(k),
+                          imove=np.full(k, WALL), iset=np.ones(k)))
+    parts.append(dict(r=np.array([[0.0, hf + probe_above]]),
+                      rho=np.array([refd]), m=np.array([0.0]), p=np.array([0.0]),
+                      imove=np.array([SENSOR]), iset=np.ones(1)))
+    # the domain holds the tank rolled by up to ~20 degrees about its bottom
+    # centre
+    cx = 0.5 * NX * dx
+    reach = float(np.hypot(cx, NY * dx)) + 8 * hfac * dx
+    params = Params(dims=2, h=hfac * dx, cs=c0, g=(0.0, -g, 0.0, 0.0),
+                    refd=(refd, refd), visc_dyn=(nu * refd, nu * refd),
+                    delta=(delta, delta),
+                    domain_min=(cx - reach, -reach, 0.0, 0.0),
+                    domain_max=(cx + reach, reach, 0.0, 0.0))
+    return _fill_case(params, parts)
+
+
+def sloshing_batch_2d(n_cases: int = 64, seed: int = 2026, dx: float = 0.004,
+                      fill_range=(0.1, 0.4), amp_deg=(2.0, 8.0),
+                      period=(1.2, 2.0), **kw) -> Batch:
+    """Independent 2-D sloshing tanks of uneven fill, each rolled
+    sinusoidally about its bottom centre with its own amplitude and period
+    (seeded: numpy.random.default_rng(seed))."""
+    rng = np.random.default_rng(seed)
+    cases, motions = [], []
+    for _ in range(n_cases):
+        fill = float(rng.uniform(*fill_range))
+        amp = float(np.deg2rad(rng.uniform(*amp_deg)))
+        T = float(rng.uniform(*period))
+        c = sloshing_tank_2d(fill, dx=dx, **kw)
+        c.dt = c.params.dt_fixed
+        cx = 0.5 * round(0.9 / dx) * dx if "tank" not in kw else 0.5 * kw["tank"][0]
+        cases.append(c)
+        motions.append(Motion(amplitude=amp, angular_freq=2.0 * math.pi / T,
+                              center=(cx, 0.0, 0.0, 0.0), iset=1))
+    return pack(cases, motions)

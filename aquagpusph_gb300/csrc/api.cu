@@ -5,6 +5,7 @@
 // 566-569): the context owns every device buffer of the resident case (two
 // sets of particle Variables that alternate between steps, plus the step
 // scratch) and allocates them all at creation; steps allocate nothing.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -14,6 +15,10 @@
 #include "kernels.cuh"
 
 using namespace aqua;
+
+namespace {
+constexpr uint32_t kMaxCases = 4096;
+}
 
 struct aqua_ctx
 {
@@ -29,6 +34,12 @@ struct aqua_ctx
     StepBufs b{};
     DevScalars* sc = nullptr;      // resident state scalars
     DevScalars* sc_aux = nullptr;  // standalone link-list / sort
+    CaseScalars* cs = nullptr;     // per-case scalars (kMaxCases)
+    CaseScalars* cs_aux = nullptr; // standalone link-list (1 case)
+    CaseMotion* cm = nullptr;      // per-case motion (kMaxCases)
+    uint32_t* offsets = nullptr;   // case offsets (kMaxCases + 1)
+    uint32_t n_cases = 1;
+    int has_motion = 0;
     uint32_t* ihoc_out = nullptr;  // ihoc export buffer (ncap)
     int extras = 0;
     int fast = 0;              // 1: -use_fast_math step kernels
@@ -149,6 +160,7 @@ layout(aqua_ctx* x, char* base)
     const int VS = (x->dims == 3) ? 4 : 2;
     for (int s = 0; s < 2; s++) {
         VarSet& v = x->set[s];
+        v.cid = cv.take<uint32_t>(n);
         v.id = cv.take<uint32_t>(n);
         v.iset = cv.take<uint32_t>(n);
         v.imove = cv.take<int32_t>(n);
@@ -192,6 +204,10 @@ layout(aqua_ctx* x, char* base)
     b.shepard = cv.take<float>(n);
     x->sc = cv.take<DevScalars>(1);
     x->sc_aux = cv.take<DevScalars>(1);
+    x->cs = cv.take<CaseScalars>(kMaxCases);
+    x->cs_aux = cv.take<CaseScalars>(1);
+    x->cm = cv.take<CaseMotion>(kMaxCases);
+    x->offsets = cv.take<uint32_t>(kMaxCases + 1);
     x->ihoc_out = cv.take<uint32_t>(x->ncap);
     return cv.off + 256;
 }
@@ -217,15 +233,20 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     const uint32_t N = x->N;
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[0], s, cudaEventRecordExternal));
-    AQ_CUDA(launch_begin(x->sc, b.cells, b.cell_wall, x->ncap, N, s));
+    AQ_CUDA(launch_begin(x->sc, x->cs, x->n_cases, b.cells, b.cell_wall,
+                         x->ncap, N, s));
     if (x->dims == 3) {
-        AQ_CUDA(launch_minmax<3>(x->consts, S.r, S.imove, N, x->sc, s));
-        AQ_CUDA(launch_icell_hist<3>(x->consts, S.r, S.imove, N, x->sc, x->ncap,
-                                     b.keys[0], b.vals[0], b.counts, s));
+        AQ_CUDA(launch_minmax<3>(x->consts, S.r, S.imove, S.cid, N, x->cs,
+                                 x->sc, s));
+        AQ_CUDA(launch_ncells<3>(x->consts, x->cs, x->n_cases, x->sc, x->ncap, s));
+        AQ_CUDA(launch_icell_hist<3>(x->consts, S.r, S.imove, S.cid, N, x->cs,
+                                     x->sc, b.keys[0], b.vals[0], b.counts, s));
     } else {
-        AQ_CUDA(launch_minmax<2>(x->consts, S.r, S.imove, N, x->sc, s));
-        AQ_CUDA(launch_icell_hist<2>(x->consts, S.r, S.imove, N, x->sc, x->ncap,
-                                     b.keys[0], b.vals[0], b.counts, s));
+        AQ_CUDA(launch_minmax<2>(x->consts, S.r, S.imove, S.cid, N, x->cs,
+                                 x->sc, s));
+        AQ_CUDA(launch_ncells<2>(x->consts, x->cs, x->n_cases, x->sc, x->ncap, s));
+        AQ_CUDA(launch_icell_hist<2>(x->consts, S.r, S.imove, S.cid, N, x->cs,
+                                     x->sc, b.keys[0], b.vals[0], b.counts, s));
     }
     AQ_CUDA(launch_radix_passes(b.keys, b.vals, N, x->passes, b.counts,
                                 b.digit_total, true, x->sc, s));
@@ -238,6 +259,9 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     a.skeys = b.keys[x->passes & 1];
     a.perm = b.vals[x->passes & 1];
     a.sc = x->sc;
+    a.cs = x->cs;
+    a.cm = x->cm;
+    a.n_cases = x->n_cases;
     a.extras = x->extras;
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[1], s, cudaEventRecordExternal));
@@ -253,7 +277,13 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
         AQ_CUDA(launch_sweep<2>(x->fast, x->consts, a, x->sweep_grid, s));
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[3], s, cudaEventRecordExternal));
-    AQ_CUDA(launch_finalize(x->sc, s));
+    AQ_CUDA(launch_finalize(x->sc, x->cs, x->cm, x->n_cases, s));
+    if (x->has_motion) {
+        if (x->dims == 3)
+            AQ_CUDA(launch_motion<3>(a, s));
+        else
+            AQ_CUDA(launch_motion<2>(a, s));
+    }
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[4], s, cudaEventRecordExternal));
     return AQUA_OK;
@@ -441,12 +471,25 @@ aqua_set_state(aqua_ctx* x, uint32_t N, const aqua_vars* v, int on_host,
     x->N = N;
     DevScalars hs;
     std::memset(&hs, 0, sizeof(hs));
-    hs.t = t;
-    hs.dt = dt;
-    hs.iter = iter;
-    hs.dt_next = 0x7f800000u;
-    // pageable source: the copy completes before the call returns
     AQ_CUDA(cudaMemcpyAsync(x->sc, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+    // one case holding every particle (aqua_set_cases() splits them)
+    CaseScalars c0;
+    std::memset(&c0, 0, sizeof(c0));
+    c0.t = t;
+    c0.dt = dt;
+    c0.iter = iter;
+    c0.dt_next = 0x7f800000u;
+    c0.cos_psi = c0.cos_psi_in = 1.f;
+    CaseMotion m0;
+    std::memset(&m0, 0, sizeof(m0));
+    const uint32_t off[2] = { 0u, N };
+    x->n_cases = 1;
+    x->has_motion = 0;
+    // pageable sources: the copies complete before the call returns
+    AQ_CUDA(cudaMemcpyAsync(x->cs, &c0, sizeof(c0), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(cudaMemcpyAsync(x->cm, &m0, sizeof(m0), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(cudaMemcpyAsync(x->offsets, off, sizeof(off), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(launch_set_case_ids(x->set[x->cur].cid, x->offsets, 1, N, s));
     AQ_CUDA(cudaStreamSynchronize(s));
     return AQUA_OK;
 }
@@ -506,21 +549,112 @@ aqua_get_extra(aqua_ctx* x, aqua_extra* e, int on_host, void* stream)
 }
 
 aqua_status
+aqua_get_case_scalars(aqua_ctx* x, uint32_t first, uint32_t count,
+                      aqua_scalars* out, void* stream)
+{
+    if (!x || !out || first + count > x->n_cases)
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    CaseScalars* h = new (std::nothrow) CaseScalars[count ? count : 1];
+    if (!h)
+        return AQUA_ERR_NO_MEMORY;
+    cudaError_t e = cudaMemcpyAsync(h, x->cs + first, count * sizeof(CaseScalars),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        delete[] h;
+        std::fprintf(stderr, "aqua_gb300: reading case scalars failed: %s\n",
+                     cudaGetErrorString(e));
+        return AQUA_ERR_CUDA;
+    }
+    for (uint32_t k = 0; k < count; k++) {
+        out[k].t = h[k].t;
+        out[k].dt = h[k].dt;
+        out[k].iter = h[k].iter;
+        std::memcpy(out[k].n_cells, h[k].n_cells, sizeof(out[k].n_cells));
+        std::memcpy(out[k].r_min, h[k].r_min, sizeof(out[k].r_min));
+        std::memcpy(out[k].r_max, h[k].r_max, sizeof(out[k].r_max));
+    }
+    delete[] h;
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_set_cases(aqua_ctx* x, uint32_t n_cases, const uint32_t* offsets,
+               const aqua_case* cases, void* stream)
+{
+    if (!x || !offsets || !cases || n_cases == 0 || n_cases > kMaxCases ||
+        offsets[0] != 0 || offsets[n_cases] != x->N)
+        return AQUA_ERR_INVALID;
+    for (uint32_t k = 0; k < n_cases; k++)
+        if (offsets[k + 1] < offsets[k])
+            return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    CaseScalars* hs = new (std::nothrow) CaseScalars[n_cases];
+    CaseMotion* hm = new (std::nothrow) CaseMotion[n_cases];
+    if (!hs || !hm) {
+        delete[] hs;
+        delete[] hm;
+        return AQUA_ERR_NO_MEMORY;
+    }
+    int motion = 0;
+    for (uint32_t k = 0; k < n_cases; k++) {
+        std::memset(&hs[k], 0, sizeof(CaseScalars));
+        std::memset(&hm[k], 0, sizeof(CaseMotion));
+        hs[k].t = cases[k].t;
+        hs[k].dt = cases[k].dt;
+        hs[k].iter = cases[k].iter;
+        hs[k].dt_next = 0x7f800000u;
+        hm[k].enabled = cases[k].roll_enabled ? 1 : 0;
+        hm[k].iset = cases[k].roll_iset;
+        hm[k].amplitude = cases[k].roll_amplitude;
+        hm[k].angular_freq = cases[k].roll_angular_freq;
+        std::memcpy(hm[k].center, cases[k].roll_center, sizeof(hm[k].center));
+        // the roll angle the boundary currently sits at: psi(t)
+        const double w = cases[k].roll_angular_freq;
+        const double A = cases[k].roll_amplitude;
+        const double psi = hm[k].enabled ? A * std::sin(w * (double)cases[k].t) : 0.0;
+        hs[k].psi = (float)psi;
+        hs[k].psi_in = hs[k].psi;
+        hs[k].omega = hm[k].enabled ? (float)(A * w * std::cos(w * (double)cases[k].t)) : 0.f;
+        hs[k].cos_psi = (float)std::cos((double)hs[k].psi);
+        hs[k].sin_psi = (float)std::sin((double)hs[k].psi);
+        hs[k].cos_psi_in = hs[k].cos_psi;
+        hs[k].sin_psi_in = hs[k].sin_psi;
+        motion |= hm[k].enabled;
+    }
+    cudaError_t e = cudaMemcpyAsync(x->cs, hs, n_cases * sizeof(CaseScalars),
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(x->cm, hm, n_cases * sizeof(CaseMotion),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(x->offsets, offsets, (n_cases + 1) * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = launch_set_case_ids(x->set[x->cur].cid, x->offsets, n_cases, x->N, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    delete[] hs;
+    delete[] hm;
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "aqua_gb300: aqua_set_cases failed: %s\n",
+                     cudaGetErrorString(e));
+        return AQUA_ERR_CUDA;
+    }
+    x->n_cases = n_cases;
+    x->has_motion = motion;
+    drop_graphs(x);
+    return AQUA_OK;
+}
+
+aqua_status
 aqua_get_scalars(aqua_ctx* x, aqua_scalars* out, void* stream)
 {
     if (!x || !out)
         return AQUA_ERR_INVALID;
-    DevScalars hs;
-    AQ_CUDA(cudaMemcpyAsync(&hs, x->sc, sizeof(hs), cudaMemcpyDeviceToHost,
-                            (cudaStream_t)stream));
-    AQ_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
-    out->t = hs.t;
-    out->dt = hs.dt;
-    out->iter = hs.iter;
-    std::memcpy(out->n_cells, hs.n_cells, sizeof(out->n_cells));
-    std::memcpy(out->r_min, hs.r_min, sizeof(out->r_min));
-    std::memcpy(out->r_max, hs.r_max, sizeof(out->r_max));
-    return AQUA_OK;
+    return aqua_get_case_scalars(x, 0, 1, out, stream);
 }
 
 aqua_status
@@ -616,15 +750,21 @@ aqua_linklist(aqua_ctx* x, const float* r_in, uint32_t N, uint32_t* icell,
     DevScalars hs;
     std::memset(&hs, 0, sizeof(hs));
     AQ_CUDA(cudaMemcpyAsync(x->sc_aux, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
-    AQ_CUDA(launch_begin(x->sc_aux, b.cells, b.cell_wall, 0, N, s));
+    AQ_CUDA(launch_begin(x->sc_aux, x->cs_aux, 1, b.cells, b.cell_wall, 0, N, s));
     if (x->dims == 3) {
-        AQ_CUDA(launch_minmax<3>(x->consts, r_in, nullptr, N, x->sc_aux, s));
-        AQ_CUDA(launch_icell_hist<3>(x->consts, r_in, nullptr, N, x->sc_aux,
-                                     ncap, b.keys[0], b.vals[0], b.counts, s));
+        AQ_CUDA(launch_minmax<3>(x->consts, r_in, nullptr, nullptr, N, x->cs_aux,
+                                 x->sc_aux, s));
+        AQ_CUDA(launch_ncells<3>(x->consts, x->cs_aux, 1, x->sc_aux, ncap, s));
+        AQ_CUDA(launch_icell_hist<3>(x->consts, r_in, nullptr, nullptr, N,
+                                     x->cs_aux, x->sc_aux, b.keys[0], b.vals[0],
+                                     b.counts, s));
     } else {
-        AQ_CUDA(launch_minmax<2>(x->consts, r_in, nullptr, N, x->sc_aux, s));
-        AQ_CUDA(launch_icell_hist<2>(x->consts, r_in, nullptr, N, x->sc_aux,
-                                     ncap, b.keys[0], b.vals[0], b.counts, s));
+        AQ_CUDA(launch_minmax<2>(x->consts, r_in, nullptr, nullptr, N, x->cs_aux,
+                                 x->sc_aux, s));
+        AQ_CUDA(launch_ncells<2>(x->consts, x->cs_aux, 1, x->sc_aux, ncap, s));
+        AQ_CUDA(launch_icell_hist<2>(x->consts, r_in, nullptr, nullptr, N,
+                                     x->cs_aux, x->sc_aux, b.keys[0], b.vals[0],
+                                     b.counts, s));
     }
     const uint32_t passes = sort_passes(bits_for(ncap));
     AQ_CUDA(launch_radix_passes(b.keys, b.vals, N, passes, b.counts,
@@ -637,14 +777,16 @@ aqua_linklist(aqua_ctx* x, const float* r_in, uint32_t N, uint32_t* icell,
     if (id_sorted)
         AQ_CUDA(launch_inverse_perm(b.vals[r], id_sorted, N, x->sc_aux, s));
     AQ_CUDA(launch_ihoc(b.keys[r], N, ihoc, ncap, x->sc_aux, s));
+    CaseScalars hc;
     AQ_CUDA(cudaMemcpyAsync(&hs, x->sc_aux, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    AQ_CUDA(cudaMemcpyAsync(&hc, x->cs_aux, sizeof(hc), cudaMemcpyDeviceToHost, s));
     AQ_CUDA(cudaStreamSynchronize(s));
     if (n_cells_host)
-        std::memcpy(n_cells_host, hs.n_cells, sizeof(hs.n_cells));
+        std::memcpy(n_cells_host, hc.n_cells, sizeof(hc.n_cells));
     if (r_min_host)
-        std::memcpy(r_min_host, hs.r_min, sizeof(hs.r_min));
+        std::memcpy(r_min_host, hc.r_min, sizeof(hc.r_min));
     if (r_max_host)
-        std::memcpy(r_max_host, hs.r_max, sizeof(hs.r_max));
+        std::memcpy(r_max_host, hc.r_max, sizeof(hc.r_max));
     if (hs.err) {
         const uint32_t zero = 0;
         AQ_CUDA(cudaMemcpyAsync(&x->sc_aux->err, &zero, 4, cudaMemcpyHostToDevice, s));
@@ -679,9 +821,9 @@ aqua_launches_per_step(aqua_ctx* x)
 {
     if (!x)
         return 0;
-    // begin, minmax, icell+hist, (passes - 1) hist, passes x (scan, scatter),
-    // gather, chunks, sweep, finalize
-    return 3u + (x->passes - 1u) + 2u * x->passes + 4u;
+    // begin, minmax, ncells, icell+hist, (passes - 1) hist,
+    // passes x (scan, scatter), gather, chunks, sweep, finalize [, motion]
+    return 4u + (x->passes - 1u) + 2u * x->passes + 4u + (x->has_motion ? 1u : 0u);
 }
 
 }  // extern "C"

@@ -45,25 +45,50 @@ struct Consts
     float q2_reject;    // |r_ij|^2 >= q2_reject  =>  |r_ij| / H >= SUPPORT
 };
 
-// Device-side scalars of the resident state
-struct DevScalars
+// Device-side scalars of one case of the resident state (a batch holds
+// n_cases independent cases, each with its own link-list and time step)
+struct CaseScalars
 {
     float r_min[4];
     float r_max[4];
     uint32_t n_cells[4];
+    uint32_t cell_base;  // first global cell key of the case
     float t;
-    float dt;          // time step of the step being run
-    uint32_t dt_next;  // bits of the running minimum of dt_var (atomicMin)
+    float dt;            // time step of the step being run
+    uint32_t dt_next;    // bits of the running minimum of dt_var (atomicMin)
     uint32_t iter;
+    float psi;           // roll angle of the moving boundary (rad)
+    float psi_in;        // roll angle of the previous step
+    float omega;         // roll rate (rad/s)
+    // cos / sin of psi and psi_in, evaluated in double and rounded
+    float cos_psi, sin_psi, cos_psi_in, sin_psi_in;
+};
+
+// Prescribed roll of a case's boundary elements and probes about `center`
+// (z axis): psi(t) = amplitude * sin(angular_freq * t)
+struct CaseMotion
+{
+    int32_t enabled;
+    uint32_t iset;       // the particle set that moves (non-fluid particles)
+    float amplitude;
+    float angular_freq;
+    float center[4];
+};
+
+// Device-side scalars shared by all cases
+struct DevScalars
+{
     uint32_t err;         // error bits
     uint32_t n_chunks;    // cell-aligned sweep chunks of this step
     uint32_t chunk_next;  // next chunk to hand out (work counter)
-    uint32_t pad;
+    uint32_t total_cells; // cells of all cases
+    uint32_t pad[4];
 };
 
 // One set of the per-particle Variables (reference layout)
 struct VarSet
 {
+    uint32_t* cid;   // case of each particle (batched runs)
     uint32_t* id;
     uint32_t* iset;
     int32_t* imove;

@@ -49,17 +49,24 @@ struct Vec<2>
     }
 };
 
-// link-list / sort launchers (linklist.cu)
-cudaError_t launch_begin(DevScalars* sc, uint2* cells, uint8_t* cell_wall,
-                         uint32_t ncap, uint32_t N, cudaStream_t s);
+// link-list / sort launchers (linklist.cu).  `cid` (case of each particle)
+// may be NULL: every particle then belongs to case 0.
+cudaError_t launch_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases,
+                         uint2* cells, uint8_t* cell_wall, uint32_t ncap,
+                         uint32_t N, cudaStream_t s);
 template<int D>
 cudaError_t launch_minmax(const Consts& c, const float* r, const int32_t* imove,
-                          uint32_t N, DevScalars* sc, cudaStream_t s);
+                          const uint32_t* cid, uint32_t N, CaseScalars* cs,
+                          DevScalars* sc, cudaStream_t s);
+template<int D>
+cudaError_t launch_ncells(const Consts& c, CaseScalars* cs, uint32_t n_cases,
+                          DevScalars* sc, uint32_t ncap, cudaStream_t s);
 template<int D>
 cudaError_t launch_icell_hist(const Consts& c, const float* r,
-                              const int32_t* imove, uint32_t N, DevScalars* sc,
-                              uint32_t ncap, uint32_t* keys, uint32_t* vals,
-                              uint32_t* counts, cudaStream_t s);
+                              const int32_t* imove, const uint32_t* cid,
+                              uint32_t N, const CaseScalars* cs, DevScalars* sc,
+                              uint32_t* keys, uint32_t* vals, uint32_t* counts,
+                              cudaStream_t s);
 cudaError_t launch_radix_passes(uint32_t* keys[2], uint32_t* vals[2],
                                 uint32_t n, uint32_t passes, uint32_t* counts,
                                 uint32_t* digit_total, bool first_counts_ready,
@@ -84,6 +91,9 @@ struct StepArgs
     const uint32_t* skeys;  // sorted cell keys
     const uint32_t* perm;   // sorted -> previous index
     DevScalars* sc;
+    CaseScalars* cs;        // per-case scalars (n_cases)
+    const CaseMotion* cm;   // per-case prescribed motion (n_cases)
+    uint32_t n_cases;
     int extras;        // write the intermediate operators
 };
 // gather / sweep of the step in the exact (IEEE, no FMA) or fast
@@ -94,7 +104,13 @@ cudaError_t launch_gather(bool fast, const Consts& c, const StepArgs& a,
 template<int D>
 cudaError_t launch_sweep(bool fast, const Consts& c, const StepArgs& a,
                          unsigned grid, cudaStream_t s);
-cudaError_t launch_finalize(DevScalars* sc, cudaStream_t s);
+cudaError_t launch_finalize(DevScalars* sc, CaseScalars* cs,
+                            const CaseMotion* cm, uint32_t n_cases,
+                            cudaStream_t s);
+template<int D>
+cudaError_t launch_motion(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_set_case_ids(uint32_t* cid, const uint32_t* offsets,
+                                uint32_t n_cases, uint32_t N, cudaStream_t s);
 cudaError_t launch_export_ihoc(const uint2* cells, uint32_t* ihoc,
                                uint32_t ncap, const DevScalars* sc,
                                cudaStream_t s);

@@ -83,18 +83,20 @@ domain_position(const Consts& c, const float* r, const int32_t* imove,
         out[k] = x[k];
 }
 
-// Resets the per-step scalars and clears the cell table.
+// Resets the per-step scalars of every case and clears the cell table.
 __global__ void
-k_begin(DevScalars* sc, uint2* cells, uint8_t* cell_wall, uint32_t ncap,
-        uint32_t N)
+k_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases, uint2* cells,
+        uint8_t* cell_wall, uint32_t ncap, uint32_t N)
 {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid == 0) {
-        for (int k = 0; k < 4; k++) {
-            sc->r_min[k] = INFINITY;
-            sc->r_max[k] = -INFINITY;
+    for (uint32_t k = tid; k < n_cases; k += gridDim.x * blockDim.x) {
+        for (int d = 0; d < 4; d++) {
+            cs[k].r_min[d] = INFINITY;
+            cs[k].r_max[d] = -INFINITY;
         }
-        sc->dt_next = __float_as_uint(INFINITY);
+        cs[k].dt_next = __float_as_uint(INFINITY);
+    }
+    if (tid == 0) {
         sc->n_chunks = 0;
         sc->chunk_next = 0;
     }
@@ -106,85 +108,98 @@ k_begin(DevScalars* sc, uint2* cells, uint8_t* cell_wall, uint32_t ncap,
     }
 }
 
-// r_min / r_max over all N particles
+// r_min / r_max of every case over its particles.  Cases are contiguous
+// runs of particles, so warps are almost always single-case: a warp
+// reduces its lanes and issues one atomic per case it touches.
 template<int D>
 __global__ void __launch_bounds__(256)
-k_minmax(Consts c, const float* r, const int32_t* imove, uint32_t N,
-         DevScalars* sc)
+k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
+         uint32_t N, CaseScalars* cs, DevScalars* sc)
 {
     constexpr int VS = Vec<D>::VS;
     if (sc->err)
         return;
-    float mn[VS], mx[VS];
-    for (int k = 0; k < VS; k++) {
-        mn[k] = INFINITY;
-        mx[k] = -INFINITY;
-    }
+    const int lane = threadIdx.x & 31;
     bool bad = false;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N;
-         i += gridDim.x * blockDim.x) {
-        float x[4];
-        bool removed;
-        domain_position<D>(c, r, imove, i, x, removed);
-        for (int k = 0; k < VS; k++) {
-            if (!isfinite(x[k])) {
+    // grid-stride over warp-sized tiles so that a warp's lanes are adjacent
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (uint32_t base = gw * 32; base < N; base += warps * 32) {
+        const uint32_t i = base + lane;
+        const bool valid = i < N;
+        float x[4] = { 0.f, 0.f, 0.f, 0.f };
+        uint32_t k = 0xffffffffu;
+        if (valid) {
+            bool removed;
+            domain_position<D>(c, r, imove, i, x, removed);
+            k = cid ? cid[i] : 0u;
+        }
+        float mn[VS], mx[VS];
+        for (int d = 0; d < VS; d++) {
+            const bool ok = valid && isfinite(x[d]);
+            if (valid && !isfinite(x[d]))
                 bad = true;
-                continue;
+            mn[d] = ok ? x[d] : INFINITY;
+            mx[d] = ok ? x[d] : -INFINITY;
+        }
+        const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+        const bool uniform = __all_sync(0xffffffffu, k == k0 || !valid);
+        if (uniform) {
+            for (int d = 0; d < VS; d++) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    mn[d] = cl_min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+                    mx[d] = cl_max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+                }
             }
-            mn[k] = cl_min(mn[k], x[k]);
-            mx[k] = cl_max(mx[k], x[k]);
-        }
-    }
-    // warp then block reduction
-    __shared__ float smn[8][VS], smx[8][VS];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = 0; k < VS; k++) {
-        for (int o = 16; o > 0; o >>= 1) {
-            mn[k] = cl_min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
-            mx[k] = cl_max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
-        }
-        if (lane == 0) {
-            smn[warp][k] = mn[k];
-            smx[warp][k] = mx[k];
+            if (lane == 0 && k0 != 0xffffffffu)
+                for (int d = 0; d < VS; d++) {
+                    atomic_min_float(&cs[k0].r_min[d], mn[d]);
+                    atomic_max_float(&cs[k0].r_max[d], mx[d]);
+                }
+        } else if (valid) {
+            for (int d = 0; d < VS; d++) {
+                atomic_min_float(&cs[k].r_min[d], mn[d]);
+                atomic_max_float(&cs[k].r_max[d], mx[d]);
+            }
         }
     }
     if (__any_sync(0xffffffffu, bad) && lane == 0)
         atomicOr(&sc->err, kErrNonFinite);
-    __syncthreads();
-    if (threadIdx.x < VS) {
-        const int k = threadIdx.x;
-        float a = smn[0][k], b = smx[0][k];
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
-            a = cl_min(a, smn[w][k]);
-            b = cl_max(b, smx[w][k]);
-        }
-        atomic_min_float(&sc->r_min[k], a);
-        atomic_max_float(&sc->r_max[k], b);
-    }
 }
 
-// n_cells from the bounding box; false (and the capacity error) if the
-// table does not fit
+// n_cells of every case from its bounding box (LinkList::nCells, float
+// division), the first global cell key of each case, and the capacity check
 template<int D>
-__device__ __forceinline__ bool
-compute_ncells(const Consts& c, const DevScalars* sc, uint32_t ncap,
-               uint32_t n[4])
+__global__ void
+k_ncells(Consts c, CaseScalars* cs, uint32_t n_cases, DevScalars* sc,
+         uint32_t ncap)
 {
-    unsigned long long nn[3] = { 1, 1, 1 };
-    for (int k = 0; k < D; k++) {
-        const float span = (sc->r_max[k] - sc->r_min[k]) / c.cell_length;
-        if (!(span >= 0.f) || span > 4.0e9f)
-            return false;
-        nn[k] = (unsigned long long)span + 6ull;
+    if (threadIdx.x != 0 || sc->err)
+        return;
+    unsigned long long base = 0;
+    for (uint32_t k = 0; k < n_cases; k++) {
+        unsigned long long nn[3] = { 1, 1, 1 };
+        bool ok = true;
+        for (int d = 0; d < D; d++) {
+            const float span = (cs[k].r_max[d] - cs[k].r_min[d]) / c.cell_length;
+            if (!(span >= 0.f) || span > 4.0e9f)
+                ok = false;
+            else
+                nn[d] = (unsigned long long)span + 6ull;
+        }
+        const unsigned long long nw = nn[0] * nn[1] * nn[2];
+        if (!ok || base + nw > ncap) {
+            atomicOr(&sc->err, kErrCapacity);
+            return;
+        }
+        cs[k].n_cells[0] = (uint32_t)nn[0];
+        cs[k].n_cells[1] = (uint32_t)nn[1];
+        cs[k].n_cells[2] = (uint32_t)nn[2];
+        cs[k].n_cells[3] = (uint32_t)nw;
+        cs[k].cell_base = (uint32_t)base;
+        base += nw;
     }
-    const unsigned long long nw = nn[0] * nn[1] * nn[2];
-    if (nw > ncap)
-        return false;
-    n[0] = (uint32_t)nn[0];
-    n[1] = (uint32_t)nn[1];
-    n[2] = (uint32_t)nn[2];
-    n[3] = (uint32_t)nw;
-    return true;
+    sc->total_cells = (uint32_t)base;
 }
 
 template<int D>
@@ -201,37 +216,18 @@ cell_of(const Consts& c, const float x[4], const float r_min[4],
     return cell;
 }
 
-// icell of every particle (keys), identity values, and the histogram of the
-// first radix digit per tile
+// icell of every particle (keys: the case's first cell + the local cell),
+// identity values, and the histogram of the first radix digit per tile
 template<int D>
 __global__ void __launch_bounds__(kSortThreads)
-k_icell_hist(Consts c, const float* r, const int32_t* imove, uint32_t N,
-             DevScalars* sc, uint32_t ncap, uint32_t* keys, uint32_t* vals,
-             uint32_t* counts, uint32_t nblocks)
+k_icell_hist(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
+             uint32_t N, const CaseScalars* cs, DevScalars* sc, uint32_t* keys,
+             uint32_t* vals, uint32_t* counts, uint32_t nblocks)
 {
     __shared__ uint32_t hist[256];
-    __shared__ uint32_t s_ok;
-    __shared__ uint32_t s_n[4];
-    __shared__ float s_min[4];
-    if (threadIdx.x == 0) {
-        uint32_t n[4];
-        const bool ok = (sc->err == 0) && compute_ncells<D>(c, sc, ncap, n);
-        s_ok = ok;
-        if (ok) {
-            for (int k = 0; k < 4; k++) {
-                s_n[k] = n[k];
-                s_min[k] = sc->r_min[k];
-            }
-            if (blockIdx.x == 0)
-                for (int k = 0; k < 4; k++)
-                    sc->n_cells[k] = n[k];
-        } else if (sc->err == 0) {
-            atomicOr(&sc->err, kErrCapacity);
-        }
-    }
     hist[threadIdx.x] = 0;
     __syncthreads();
-    if (!s_ok)
+    if (sc->err)
         return;
     const uint32_t base = blockIdx.x * kSortTile;
     for (int it = 0; it < kSortItems; it++) {
@@ -241,7 +237,8 @@ k_icell_hist(Consts c, const float* r, const int32_t* imove, uint32_t N,
         float x[4];
         bool removed;
         domain_position<D>(c, r, imove, i, x, removed);
-        const uint32_t key = cell_of<D>(c, x, s_min, s_n);
+        const CaseScalars& k = cs[cid ? cid[i] : 0u];
+        const uint32_t key = k.cell_base + cell_of<D>(c, x, k.r_min, k.n_cells);
         keys[i] = key;
         vals[i] = i;
         atomicAdd(&hist[key & 255u], 1u);
@@ -477,21 +474,31 @@ grid_for(uint32_t n, unsigned threads)
 }
 
 cudaError_t
-launch_begin(DevScalars* sc, uint2* cells, uint8_t* cell_wall, uint32_t ncap,
-             uint32_t N, cudaStream_t s)
+launch_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases, uint2* cells,
+             uint8_t* cell_wall, uint32_t ncap, uint32_t N, cudaStream_t s)
 {
-    const unsigned g = min(grid_for(ncap, 256), 152u * 8u);
-    k_begin<<<max(g, 1u), 256, 0, s>>>(sc, cells, cell_wall, ncap, N);
+    const unsigned g = min(grid_for(max(ncap, n_cases), 256), 152u * 8u);
+    k_begin<<<max(g, 1u), 256, 0, s>>>(sc, cs, n_cases, cells, cell_wall, ncap, N);
     return cudaGetLastError();
 }
 
 template<int D>
 cudaError_t
 launch_minmax(const Consts& c, const float* r, const int32_t* imove,
-              uint32_t N, DevScalars* sc, cudaStream_t s)
+              const uint32_t* cid, uint32_t N, CaseScalars* cs, DevScalars* sc,
+              cudaStream_t s)
 {
     const unsigned g = min(grid_for(N, 256), 152u * 4u);
-    k_minmax<D><<<max(g, 1u), 256, 0, s>>>(c, r, imove, N, sc);
+    k_minmax<D><<<max(g, 1u), 256, 0, s>>>(c, r, imove, cid, N, cs, sc);
+    return cudaGetLastError();
+}
+
+template<int D>
+cudaError_t
+launch_ncells(const Consts& c, CaseScalars* cs, uint32_t n_cases, DevScalars* sc,
+              uint32_t ncap, cudaStream_t s)
+{
+    k_ncells<D><<<1, 32, 0, s>>>(c, cs, n_cases, sc, ncap);
     return cudaGetLastError();
 }
 
@@ -534,14 +541,15 @@ launch_radix_passes(uint32_t* keys[2], uint32_t* vals[2], uint32_t n,
 template<int D>
 cudaError_t
 launch_icell_hist(const Consts& c, const float* r, const int32_t* imove,
-                  uint32_t N, DevScalars* sc, uint32_t ncap, uint32_t* keys,
-                  uint32_t* vals, uint32_t* counts, cudaStream_t s)
+                  const uint32_t* cid, uint32_t N, const CaseScalars* cs,
+                  DevScalars* sc, uint32_t* keys, uint32_t* vals,
+                  uint32_t* counts, cudaStream_t s)
 {
     const uint32_t nb = sort_blocks(N);
     if (nb == 0)
         return cudaSuccess;
-    k_icell_hist<D><<<nb, kSortThreads, 0, s>>>(c, r, imove, N, sc, ncap, keys,
-                                                 vals, counts, nb);
+    k_icell_hist<D><<<nb, kSortThreads, 0, s>>>(c, r, imove, cid, N, cs, sc,
+                                                 keys, vals, counts, nb);
     return cudaGetLastError();
 }
 
@@ -575,18 +583,24 @@ launch_iota(uint32_t* p, uint32_t n, cudaStream_t s)
 }
 
 template cudaError_t launch_minmax<2>(const Consts&, const float*,
-                                      const int32_t*, uint32_t, DevScalars*,
-                                      cudaStream_t);
+                                      const int32_t*, const uint32_t*, uint32_t,
+                                      CaseScalars*, DevScalars*, cudaStream_t);
 template cudaError_t launch_minmax<3>(const Consts&, const float*,
-                                      const int32_t*, uint32_t, DevScalars*,
-                                      cudaStream_t);
+                                      const int32_t*, const uint32_t*, uint32_t,
+                                      CaseScalars*, DevScalars*, cudaStream_t);
+template cudaError_t launch_ncells<2>(const Consts&, CaseScalars*, uint32_t,
+                                      DevScalars*, uint32_t, cudaStream_t);
+template cudaError_t launch_ncells<3>(const Consts&, CaseScalars*, uint32_t,
+                                      DevScalars*, uint32_t, cudaStream_t);
 template cudaError_t launch_icell_hist<2>(const Consts&, const float*,
-                                          const int32_t*, uint32_t,
-                                          DevScalars*, uint32_t, uint32_t*,
-                                          uint32_t*, uint32_t*, cudaStream_t);
+                                          const int32_t*, const uint32_t*,
+                                          uint32_t, const CaseScalars*,
+                                          DevScalars*, uint32_t*, uint32_t*,
+                                          uint32_t*, cudaStream_t);
 template cudaError_t launch_icell_hist<3>(const Consts&, const float*,
-                                          const int32_t*, uint32_t,
-                                          DevScalars*, uint32_t, uint32_t*,
-                                          uint32_t*, uint32_t*, cudaStream_t);
+                                          const int32_t*, const uint32_t*,
+                                          uint32_t, const CaseScalars*,
+                                          DevScalars*, uint32_t*, uint32_t*,
+                                          uint32_t*, cudaStream_t);
 
 }  // namespace aqua

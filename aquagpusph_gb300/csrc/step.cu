@@ -39,26 +39,142 @@ k_chunks(const uint32_t* skeys, const uint2* cells, uint32_t N, uint2* chunks,
         chunks[base + __popc(b & ((1u << lane) - 1u))] = w;
 }
 
+// End of step of every case: dt = min(dt_var) (Reduction tool), assert
+// dt > 0, t += dt, iter += 1 (set_scalar tools); for a rolling case, the new
+// roll angle and rate at the new time (the reference's motion tools run
+// after the time step, cfd/motion.xml:59-71).
 __global__ void
-k_finalize(DevScalars* sc)
+k_finalize(DevScalars* sc, CaseScalars* cs, const CaseMotion* cm,
+           uint32_t n_cases)
 {
     if (sc->err)
         return;
-    const float dt = __uint_as_float(sc->dt_next);
-    if (!(dt > 0.f) || isinf(dt)) {
-        atomicOr(&sc->err, kErrDt);
-        return;
+    for (uint32_t k = threadIdx.x; k < n_cases; k += blockDim.x) {
+        CaseScalars& c = cs[k];
+        const float dt = __uint_as_float(c.dt_next);
+        if (!(dt > 0.f) || isinf(dt)) {
+            atomicOr(&sc->err, kErrDt);
+            continue;
+        }
+        c.dt = dt;
+        c.t = (float)((double)c.t + (double)dt);
+        c.iter = c.iter + 1;
+        if (cm[k].enabled) {
+            const double w = (double)cm[k].angular_freq;
+            const double A = (double)cm[k].amplitude;
+            const double psi = A * sin(w * (double)c.t);
+            c.psi_in = c.psi;
+            c.cos_psi_in = c.cos_psi;
+            c.sin_psi_in = c.sin_psi;
+            c.psi = (float)psi;
+            c.omega = (float)(A * w * cos(w * (double)c.t));
+            c.cos_psi = (float)cos((double)c.psi);
+            c.sin_psi = (float)sin((double)c.psi);
+        }
     }
-    sc->dt = dt;
-    sc->t = (float)((double)sc->t + (double)dt);
-    sc->iter = sc->iter + 1;
+}
+
+// Prescribed roll of the boundary elements and probes of a moving case
+// about `center` (z axis): un-transform with the previous angle, velocity
+// from the new rate, transform with the new angle
+// (cfd/Motions/UnTransform.cl, Velocity.cl, Transform.cl).
+template<int D>
+__global__ void __launch_bounds__(256)
+k_motion(StepArgs a)
+{
+    constexpr int VS = Vec<D>::VS;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.N || a.sc->err)
+        return;
+    const VarSet& T = a.dst;
+    const uint32_t k = T.cid[i];
+    const CaseMotion& m = a.cm[k];
+    if (!m.enabled || T.iset[i] != m.iset || T.imove[i] == 1)
+        return;
+    const CaseScalars& c = a.cs[k];
+    float r[4], n[4], t[4];
+    Vec<D>::load(T.r, i, r);
+    Vec<D>::load(T.normal, i, n);
+    Vec<D>::load(T.tangent, i, t);
+    // un-transform (rotation by -psi_in about z, around the centre)
+    for (int d = 0; d < VS; d++)
+        r[d] = r[d] - m.center[d];
+    const float ci = c.cos_psi_in, si = -c.sin_psi_in;
+    float rl[4], nl[4], tl[4];
+    for (int d = 0; d < 4; d++) {
+        rl[d] = r[d];
+        nl[d] = n[d];
+        tl[d] = t[d];
+    }
+    rl[0] = ci * r[0] - si * r[1];
+    rl[1] = si * r[0] + ci * r[1];
+    nl[0] = ci * n[0] - si * n[1];
+    nl[1] = si * n[0] + ci * n[1];
+    tl[0] = ci * t[0] - si * t[1];
+    tl[1] = si * t[0] + ci * t[1];
+    // velocity of the rotation in the local frame, then rotated
+    const float cp = c.cos_psi, sp = c.sin_psi;
+    float ul[4] = { 0.f, 0.f, 0.f, 0.f }, u[4] = { 0.f, 0.f, 0.f, 0.f };
+    ul[0] = -c.omega * rl[1];
+    ul[1] = c.omega * rl[0];
+    u[0] = cp * ul[0] - sp * ul[1];
+    u[1] = sp * ul[0] + cp * ul[1];
+    // transform with the new angle
+    float ro[4], no[4], to[4];
+    for (int d = 0; d < 4; d++) {
+        ro[d] = rl[d];
+        no[d] = nl[d];
+        to[d] = tl[d];
+    }
+    ro[0] = cp * rl[0] - sp * rl[1];
+    ro[1] = sp * rl[0] + cp * rl[1];
+    no[0] = cp * nl[0] - sp * nl[1];
+    no[1] = sp * nl[0] + cp * nl[1];
+    to[0] = cp * tl[0] - sp * tl[1];
+    to[1] = sp * tl[0] + cp * tl[1];
+    for (int d = 0; d < VS; d++)
+        ro[d] = ro[d] + m.center[d];
+    float nn = 0.f, tt = 0.f;
+    for (int d = 0; d < VS; d++) {
+        nn = nn + no[d] * no[d];
+        tt = tt + to[d] * to[d];
+    }
+    nn = sqrtf(nn);
+    tt = sqrtf(tt);
+    for (int d = 0; d < VS; d++) {
+        no[d] = no[d] / nn;
+        to[d] = to[d] / tt;
+    }
+    Vec<D>::store(T.r, i, ro);
+    Vec<D>::store(T.normal, i, no);
+    Vec<D>::store(T.tangent, i, to);
+    Vec<D>::store(T.u, i, u);
+}
+
+// case id of every particle from the case offsets
+__global__ void
+k_set_case_ids(uint32_t* cid, const uint32_t* offsets, uint32_t n_cases,
+               uint32_t N)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N)
+        return;
+    uint32_t lo = 0, hi = n_cases;  // offsets[lo] <= i < offsets[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (offsets[mid] <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    cid[i] = lo;
 }
 
 __global__ void
 k_export_ihoc(const uint2* cells, uint32_t* ihoc, uint32_t ncap,
               const DevScalars* sc)
 {
-    const uint32_t nw = sc->n_cells[3];
+    const uint32_t nw = sc->total_cells;
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncap && c < nw;
          c += gridDim.x * blockDim.x)
         ihoc[c] = cells[c].x;
@@ -91,9 +207,30 @@ launch_sweep(bool fast, const Consts& c, const StepArgs& a, unsigned grid,
 }
 
 cudaError_t
-launch_finalize(DevScalars* sc, cudaStream_t s)
+launch_finalize(DevScalars* sc, CaseScalars* cs, const CaseMotion* cm,
+                uint32_t n_cases, cudaStream_t s)
 {
-    k_finalize<<<1, 1, 0, s>>>(sc);
+    k_finalize<<<1, 256, 0, s>>>(sc, cs, cm, n_cases);
+    return cudaGetLastError();
+}
+
+template<int D>
+cudaError_t
+launch_motion(const StepArgs& a, cudaStream_t s)
+{
+    if (a.N == 0)
+        return cudaSuccess;
+    k_motion<D><<<(a.N + 255) / 256, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t
+launch_set_case_ids(uint32_t* cid, const uint32_t* offsets, uint32_t n_cases,
+                    uint32_t N, cudaStream_t s)
+{
+    if (N == 0)
+        return cudaSuccess;
+    k_set_case_ids<<<(N + 255) / 256, 256, 0, s>>>(cid, offsets, n_cases, N);
     return cudaGetLastError();
 }
 
@@ -106,6 +243,8 @@ launch_export_ihoc(const uint2* cells, uint32_t* ihoc, uint32_t ncap,
     return cudaGetLastError();
 }
 
+template cudaError_t launch_motion<2>(const StepArgs&, cudaStream_t);
+template cudaError_t launch_motion<3>(const StepArgs&, cudaStream_t);
 template cudaError_t launch_gather<2>(bool, const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_gather<3>(bool, const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_sweep<2>(bool, const Consts&, const StepArgs&, unsigned,

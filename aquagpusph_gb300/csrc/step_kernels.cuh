@@ -175,8 +175,10 @@ k_gather(Consts c, StepArgs a)
 
     const VarSet& S = a.src;
     const VarSet& T = a.dst;
-    const float dt = a.sc->dt;
+    const uint32_t kc = S.cid[o];
+    const float dt = a.cs[kc].dt;
     const float hdt = 0.5f * dt;
+    T.cid[s] = kc;
 
     // Domain (on the predictor backups) + sort stage1
     int im = S.imove[o];
@@ -286,13 +288,14 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
 {
     constexpr int VS = Vec<D>::VS;
     constexpr int NC = (D == 3) ? 27 : 9;
-    const float dt = a.sc->dt;
+    const VarSet& T = a.dst;
+    const CaseScalars& cas = a.cs[T.cid[i]];
+    const float dt = cas.dt;
     const float hdt = 0.5f * dt;
     const float4 pi = a.b.posq[i];
     const int im = __float_as_int(pi.w);
-    const VarSet& T = a.dst;
-    const uint32_t nx = a.sc->n_cells[0];
-    const uint32_t nxy = a.sc->n_cells[0] * a.sc->n_cells[1];
+    const uint32_t nx = cas.n_cells[0];
+    const uint32_t nxy = cas.n_cells[0] * cas.n_cells[1];
     const uint32_t key_i = a.skeys[i];
     const bool fluid = valid && (im == 1), sensor = valid && (im == 0);
     const bool want_shep = valid && (im >= -3) && (im <= 1);
@@ -630,11 +633,21 @@ template<int D>
 __global__ void __launch_bounds__(kSweepThreads, 5)
 k_sweep(Consts c, StepArgs a)
 {
-    __shared__ float s_dtmin[kSweepThreads / 32];
     __shared__ uint16_t s_queue[kSweepQueue * kSweepThreads];
     __shared__ uint32_t s_cstart[kSweepThreads / 32][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float dt_min = INFINITY;
+    // running minimum of dt_var of the warp's current case, flushed to the
+    // case's dt_next when the case changes and at the end
+    float run_min = INFINITY;
+    uint32_t run_case = 0xffffffffu;
+    auto flush = [&]() {
+        if (lane == 0 && run_case != 0xffffffffu) {
+            if (run_min < INFINITY && run_min >= 0.f)
+                atomicMin(&a.cs[run_case].dt_next, __float_as_uint(run_min));
+            else if (!(run_min >= 0.f))
+                atomicOr(&a.sc->err, kErrDt);
+        }
+    };
     if (a.sc->err == 0) {
         const uint32_t nch = a.sc->n_chunks;
         for (;;) {
@@ -646,28 +659,21 @@ k_sweep(Consts c, StepArgs a)
                 break;
             const uint2 cw = a.b.chunks[ch];
             const bool valid = (uint32_t)lane < cw.y;
-            const float v = sweep_particle<D>(c, a, valid ? cw.x + lane : cw.x,
-                                              valid, s_queue + threadIdx.x,
-                                              s_cstart[warp]);
+            float v = sweep_particle<D>(c, a, valid ? cw.x + lane : cw.x, valid,
+                                        s_queue + threadIdx.x, s_cstart[warp]);
             __syncwarp();  // s_cstart is rewritten for the next chunk
-            dt_min = cl_min(dt_min, v);
+            for (int o = 16; o > 0; o >>= 1)
+                v = cl_min(v, __shfl_xor_sync(0xffffffffu, v, o));
+            const uint32_t kc = a.dst.cid[cw.x];
+            if (kc != run_case) {
+                flush();
+                run_case = kc;
+                run_min = INFINITY;
+            }
+            run_min = cl_min(run_min, v);
         }
     }
-    // block minimum of dt_var, one atomic per block
-    for (int o = 16; o > 0; o >>= 1)
-        dt_min = cl_min(dt_min, __shfl_xor_sync(0xffffffffu, dt_min, o));
-    if (lane == 0)
-        s_dtmin[warp] = dt_min;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float m = s_dtmin[0];
-        for (int w = 1; w < kSweepThreads / 32; w++)
-            m = cl_min(m, s_dtmin[w]);
-        if (m < INFINITY && m >= 0.f)
-            atomicMin(&a.sc->dt_next, __float_as_uint(m));
-        else if (!(m >= 0.f))
-            atomicOr(&a.sc->err, kErrDt);
-    }
+    flush();
 }
 
 template<int D>

@@ -99,6 +99,36 @@ class Solver:
         self.set_state_raw(case.N, arrays, True, case.t, case.dt, case.iter,
                            stream)
         self._case = case
+        self.n_cases = 1
+
+    def set_batch(self, batch, stream=None):
+        """Loads a :class:`aquagpusph_gb300.case.Batch`: its concatenated
+        particles, then the split into independent cases (aqua_set_cases)."""
+        self.set_case(batch.case, stream)
+        n = len(batch.offsets) - 1
+        offs = np.ascontiguousarray(batch.offsets, np.uint32)
+        arr = (_lib.AquaCase * n)()
+        for k, m in enumerate(batch.motions):
+            a = arr[k]
+            a.t, a.dt, a.iter = batch.case.t, batch.case.dt, batch.case.iter
+            if m is not None:
+                a.roll_enabled = 1
+                a.roll_iset = m.iset
+                a.roll_amplitude = m.amplitude
+                a.roll_angular_freq = m.angular_freq
+                a.roll_center[:] = (list(m.center) + [0.0] * 4)[:4]
+        _lib.check("aqua_set_cases", self.lib.aqua_set_cases(
+            self.ctx, n, offs.ctypes.data_as(_lib._U), arr,
+            C.c_void_p(stream or 0)))
+        self.n_cases = n
+
+    def case_scalars(self, stream=None) -> list:
+        n = getattr(self, "n_cases", 1)
+        out = (_lib.AquaScalars * n)()
+        _lib.check("aqua_get_case_scalars", self.lib.aqua_get_case_scalars(
+            self.ctx, 0, n, out, C.c_void_p(stream or 0)))
+        return [{"t": s.t, "dt": s.dt, "iter": s.iter,
+                 "n_cells": np.array(s.n_cells[:], np.uint32)} for s in out]
 
     def step(self, n: int = 1, graph: bool = True, stream=None):
         _lib.check("aqua_step", self.lib.aqua_step(

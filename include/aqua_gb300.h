@@ -135,6 +135,24 @@ typedef struct
     float r_max[4];
 } aqua_scalars;
 
+/* One case of a batch: its scalars and an optional prescribed roll of its
+ * boundary elements and probes (particles of set `roll_iset` that are not
+ * fluid) about the z axis through `roll_center`:
+ * psi(t) = roll_amplitude * sin(roll_angular_freq * t).  The motion is
+ * applied at the end of every step, after the time step, as the reference's
+ * motion preset does (cfd/motion.xml:59-71). */
+typedef struct
+{
+    float t;
+    float dt;
+    uint32_t iter;
+    int32_t roll_enabled;
+    uint32_t roll_iset;
+    float roll_amplitude;     /* rad */
+    float roll_angular_freq;  /* rad/s */
+    float roll_center[4];
+} aqua_case;
+
 typedef struct aqua_ctx aqua_ctx;
 
 /* Library version string */
@@ -177,6 +195,18 @@ aqua_status aqua_set_precision(aqua_ctx* ctx, int mode);
 aqua_status aqua_set_state(aqua_ctx* ctx, uint32_t N, const aqua_vars* src,
                            int on_host, float t, float dt, uint32_t iter,
                            void* stream);
+
+/* Splits the resident particles (uploaded by aqua_set_state) into n_cases
+ * independent cases: case k holds particles [offsets[k], offsets[k+1]).
+ * Every case gets its own bounding box, cell grid, sort keys, time step and
+ * time; one aqua_step() advances all of them (one launch per kernel for the
+ * whole batch).  Host arrays; at most 4096 cases. */
+aqua_status aqua_set_cases(aqua_ctx* ctx, uint32_t n_cases,
+                           const uint32_t* offsets, const aqua_case* cases,
+                           void* stream);
+/* Scalars of cases [first, first+count) (synchronises `stream`). */
+aqua_status aqua_get_case_scalars(aqua_ctx* ctx, uint32_t first, uint32_t count,
+                                  aqua_scalars* out, void* stream);
 
 /* Copies the resident state out (any non-NULL field is written). */
 aqua_status aqua_get_state(aqua_ctx* ctx, aqua_vars* dst, int on_host,

@@ -251,6 +251,82 @@ linklist(Case<D>& cs)
     return AQ_OK;
 }
 
+/* ------------------------------------------------------ prescribed roll */
+
+/* Rolls the boundary elements and probes of the roll set from the angle at
+ * t_before to the angle at t_after about z through roll_center: the
+ * reference's motion tools UnTransform (previous angle), Velocity and
+ * Transform (new angle), cfd/Motions/{UnTransform,Velocity,Transform}.cl.
+ * Angles, rate, cosines and sines are evaluated in double and rounded. */
+template<int D>
+void
+roll(Case<D>& cs, float t_before, float t_after)
+{
+    aq_state* st = cs.st;
+    const aq_params* pr = cs.pr;
+    const int VS = Case<D>::VS;
+    const double w = pr->roll_angular_freq, A = pr->roll_amplitude;
+    const float psi_in = (float)(A * std::sin(w * (double)t_before));
+    const float psi = (float)(A * std::sin(w * (double)t_after));
+    const float omega = (float)(A * w * std::cos(w * (double)t_after));
+    const float ci = (float)std::cos((double)psi_in);
+    const float si = -(float)std::sin((double)psi_in);
+    const float cp = (float)std::cos((double)psi);
+    const float sp = (float)std::sin((double)psi);
+    par_for(cs.N, cs.nt, [&](uint32_t i) {
+        if (st->iset[i] != pr->roll_iset || st->imove[i] == 1)
+            return;
+        float* r = cs.vec(st->r, i);
+        float* n = cs.vec(st->normal, i);
+        float* t = cs.vec(st->tangent, i);
+        float* u = cs.vec(st->u, i);
+        float rr[4] = { 0.f, 0.f, 0.f, 0.f };
+        for (int d = 0; d < VS; d++)
+            rr[d] = r[d] - pr->roll_center[d];
+        float rl[4], nl[4], tl[4];
+        for (int d = 0; d < 4; d++) {
+            rl[d] = d < VS ? rr[d] : 0.f;
+            nl[d] = d < VS ? n[d] : 0.f;
+            tl[d] = d < VS ? t[d] : 0.f;
+        }
+        rl[0] = ci * rr[0] - si * rr[1];
+        rl[1] = si * rr[0] + ci * rr[1];
+        nl[0] = ci * n[0] - si * n[1];
+        nl[1] = si * n[0] + ci * n[1];
+        tl[0] = ci * t[0] - si * t[1];
+        tl[1] = si * t[0] + ci * t[1];
+        const float ul0 = -omega * rl[1], ul1 = omega * rl[0];
+        float ro[4], no[4], to[4];
+        for (int d = 0; d < 4; d++) {
+            ro[d] = rl[d];
+            no[d] = nl[d];
+            to[d] = tl[d];
+        }
+        ro[0] = cp * rl[0] - sp * rl[1];
+        ro[1] = sp * rl[0] + cp * rl[1];
+        no[0] = cp * nl[0] - sp * nl[1];
+        no[1] = sp * nl[0] + cp * nl[1];
+        to[0] = cp * tl[0] - sp * tl[1];
+        to[1] = sp * tl[0] + cp * tl[1];
+        float nn = 0.f, tt = 0.f;
+        for (int d = 0; d < VS; d++) {
+            ro[d] = ro[d] + pr->roll_center[d];
+            nn = nn + no[d] * no[d];
+            tt = tt + to[d] * to[d];
+        }
+        nn = std::sqrt(nn);
+        tt = std::sqrt(tt);
+        for (int d = 0; d < VS; d++) {
+            r[d] = ro[d];
+            n[d] = no[d] / nn;
+            t[d] = to[d] / tt;
+            u[d] = 0.f;
+        }
+        u[0] = cp * ul0 - sp * ul1;
+        u[1] = sp * ul0 + cp * ul1;
+    });
+}
+
 /* --------------------------------------------------------- one step */
 
 template<int D>
@@ -688,8 +764,11 @@ step(Case<D>& cs)
     if (!(dt_new > 0.f))
         return AQ_ERR_DT;
     st->dt = dt_new;
+    const float t_before = st->t;
     st->t = (float)((double)st->t + (double)dt_new);
     st->iter += 1;
+    if (pr->roll_enabled)
+        roll<D>(cs, t_before, st->t);
     return AQ_OK;
 }
 

@@ -55,6 +55,16 @@ typedef struct
     const float* refd;
     const float* visc_dyn;
     const float* delta;
+    /* prescribed roll of the boundary elements and probes (non-fluid
+     * particles of set roll_iset) about z through roll_center:
+     * psi(t) = roll_amplitude * sin(roll_angular_freq * t), applied after the
+     * time step (cfd/motion.xml:59-71); the reference-kernel harness ignores
+     * these fields */
+    int32_t roll_enabled;
+    uint32_t roll_iset;
+    float roll_amplitude;
+    float roll_angular_freq;
+    float roll_center[4];
 } aq_params;
 
 /* Particle Variables (host pointers). */

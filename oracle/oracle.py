@@ -44,6 +44,9 @@ class AqParams(C.Structure):
         ("dr_factor", C.c_float), ("min_bound_dist", C.c_float),
         ("relax_midpoint", C.c_float), ("iter_midpoint_max", C.c_uint32),
         ("refd", _F), ("visc_dyn", _F), ("delta", _F),
+        ("roll_enabled", C.c_int32), ("roll_iset", C.c_uint32),
+        ("roll_amplitude", C.c_float), ("roll_angular_freq", C.c_float),
+        ("roll_center", C.c_float * 4),
     ]
 
 
@@ -76,9 +79,10 @@ class AqState(C.Structure):
                  ("dt", C.c_float), ("iter", C.c_uint32)])
 
 
-def make_params(p) -> tuple:
-    """AqParams from a :class:`aquagpusph_gb300.case.Params`; returns the
-    structure and the arrays it points into (keep them alive)."""
+def make_params(p, motion=None) -> tuple:
+    """AqParams from a :class:`aquagpusph_gb300.case.Params` (and an optional
+    :class:`aquagpusph_gb300.case.Motion`); returns the structure and the
+    arrays it points into (keep them alive)."""
     keep = [np.ascontiguousarray(np.asarray(a, np.float32))
             for a in (p.refd, p.visc_dyn, p.delta)]
     s = AqParams()
@@ -98,6 +102,12 @@ def make_params(p) -> tuple:
     s.relax_midpoint = p.relax_midpoint
     s.iter_midpoint_max = p.iter_midpoint_max
     s.refd, s.visc_dyn, s.delta = (a.ctypes.data_as(_F) for a in keep)
+    if motion is not None:
+        s.roll_enabled = 1
+        s.roll_iset = motion.iset
+        s.roll_amplitude = motion.amplitude
+        s.roll_angular_freq = motion.angular_freq
+        s.roll_center[:] = (list(motion.center) + [0.0] * 4)[:4]
     return s, keep
 
 
@@ -164,8 +174,8 @@ class Oracle:
         self.lib.aq_sort.argtypes = [_U, _U, _U, C.c_uint32]
         self.lib.aq_sort.restype = C.c_int
 
-    def step(self, st: OracleState, nthreads=0, steps=1):
-        p, keep = make_params(st.case.params)
+    def step(self, st: OracleState, nthreads=0, steps=1, motion=None):
+        p, keep = make_params(st.case.params, motion)
         for _ in range(steps):
             err = self.lib.aq_step(C.byref(st.s), C.byref(p), nthreads)
             if err:

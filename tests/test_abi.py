@@ -51,5 +51,10 @@ def test_binding_covers_header(lib_path):
 def test_structs_match_between_oracle_and_library():
     import oracle as O
     from aquagpusph_gb300 import _lib
-    assert ctypes.sizeof(O.AqParams) == ctypes.sizeof(_lib.AquaParams)
-    assert [f[0] for f in O.AqParams._fields_] == [f[0] for f in _lib.AquaParams._fields_]
+    # the library's aqua_params is the leading part of the oracle's aq_params
+    # (the oracle adds the per-case roll fields that the library keeps in
+    # aqua_case)
+    lib_fields = [f[0] for f in _lib.AquaParams._fields_]
+    assert [f[0] for f in O.AqParams._fields_][: len(lib_fields)] == lib_fields
+    for name in lib_fields:
+        assert getattr(O.AqParams, name).offset == getattr(_lib.AquaParams, name).offset
