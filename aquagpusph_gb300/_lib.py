@@ -104,6 +104,7 @@ SIGNATURES = [
     ("aqua_set_params", C.c_int, [C.c_void_p, C.POINTER(AquaParams)]),
     ("aqua_set_extras", C.c_int, [C.c_void_p, C.c_int]),
     ("aqua_set_precision", C.c_int, [C.c_void_p, C.c_int]),
+    ("aqua_set_tuning", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     ("aqua_set_state", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(AquaVars),
                                  C.c_int, C.c_float, C.c_float, C.c_uint32,
                                  C.c_void_p]),

@@ -1,0 +1,118 @@
+"""Launch-shape tuner of the sweep kernel.
+
+The sweep can run with different block sizes (threads per block = how many
+cell-aligned 32-particle chunks a block holds), queue depths (neighbours each
+thread stages before the pair arithmetic) and persistent-grid sizes (blocks
+per SM).  Every choice gives the same results; the fastest depends on the
+GPU and on the case (particles per cell, wall fraction, batch size).
+:func:`autotune` times each candidate on the live case with a few steps and
+keeps the fastest; the choice is cached per (GPU, case signature) in a JSON
+file so later runs of the same configuration skip the search.
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+
+from . import _lib
+
+# (variant, threads per block, queued neighbours per thread); the variant
+# numbers are those of aqua_set_tuning
+VARIANTS = ((0, 128, 128), (1, 64, 128), (2, 128, 64), (3, 256, 64))
+BLOCKS_PER_SM = (2, 3, 4, 5, 6, 8, 10)
+MAX_THREADS_PER_SM = 2048
+
+
+def cache_path() -> str:
+    return os.environ.get(
+        "AQUA_TUNE_CACHE",
+        os.path.join(os.path.expanduser("~"), ".cache", "aquagpusph_gb300",
+                     "tuning.json"))
+
+
+def gpu_name() -> str:
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.cuda.get_device_name(torch.cuda.current_device())
+    except Exception:
+        pass
+    return "cuda"
+
+
+def signature(solver, fast: bool) -> str:
+    p = solver.params
+    n_cases = getattr(solver, "n_cases", 1)
+    # particle counts bucketed to 1/16 of a power of two
+    n = max(solver.N, 1)
+    bucket = 1 << (n.bit_length() - 1)
+    bucket = bucket + ((n - bucket) // (bucket // 16 or 1)) * (bucket // 16 or 1)
+    return (f"{gpu_name()}|dims={p.dims}|N~{bucket}|cases={n_cases}|"
+            f"h={p.h:.6g}|{'fast' if fast else 'exact'}")
+
+
+def _load():
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(d):
+    path = cache_path()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+
+
+def candidates():
+    for v, threads, queue in VARIANTS:
+        for b in BLOCKS_PER_SM:
+            if b * threads <= MAX_THREADS_PER_SM:
+                yield v, b
+
+
+def autotune(solver, fast: bool, steps: int = 3, use_cache: bool = True,
+             stream=None) -> dict:
+    """Picks the fastest sweep launch shape for the solver's resident case
+    and applies it.  Advances the resident state by the timed steps (call it
+    during warm-up, or restore the state afterwards)."""
+    key = signature(solver, fast)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        v, b = cache[key]["variant"], cache[key]["blocks_per_sm"]
+        solver.set_tuning(v, b)
+        return dict(cache[key], cached=True)
+    results = []
+    for v, b in candidates():
+        try:
+            solver.set_tuning(v, b)
+        except _lib.AquaError:
+            continue
+        solver.step(1, graph=True, stream=stream)      # capture + warm
+        solver.scalars(stream)
+        t0 = time.perf_counter()
+        solver.step(steps, graph=True, stream=stream)
+        solver.scalars(stream)                         # synchronises
+        dt = (time.perf_counter() - t0) / steps
+        results.append((dt, v, b))
+    solver.check(stream)
+    results.sort()
+    best_dt, v, b = results[0]
+    solver.set_tuning(v, b)
+    entry = {"variant": v, "blocks_per_sm": b,
+             "threads": dict((x[0], x[1]) for x in VARIANTS)[v],
+             "queue": dict((x[0], x[2]) for x in VARIANTS)[v],
+             "ms_per_step": 1e3 * best_dt,
+             "candidates": [[round(1e3 * d, 4), vv, bb] for d, vv, bb in results]}
+    if use_cache:
+        cache[key] = entry
+        _save(cache)
+    return dict(entry, cached=False)

@@ -44,6 +44,8 @@ struct aqua_ctx
     int extras = 0;
     int fast = 0;              // 1: -use_fast_math step kernels
     unsigned sweep_grid = 0;   // persistent sweep blocks
+    int sweep_variant = 0;     // block size / queue depth of the sweep
+    int sms = 1;
     void* pool = nullptr;
     size_t pool_bytes = 0;
     cudaStream_t cap_stream = nullptr;
@@ -272,9 +274,11 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[2], s, cudaEventRecordExternal));
     if (x->dims == 3)
-        AQ_CUDA(launch_sweep<3>(x->fast, x->consts, a, x->sweep_grid, s));
+        AQ_CUDA(launch_sweep<3>(x->fast, x->consts, a, x->sweep_grid,
+                                x->sweep_variant, s));
     else
-        AQ_CUDA(launch_sweep<2>(x->fast, x->consts, a, x->sweep_grid, s));
+        AQ_CUDA(launch_sweep<2>(x->fast, x->consts, a, x->sweep_grid,
+                                x->sweep_variant, s));
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[3], s, cudaEventRecordExternal));
     AQ_CUDA(launch_finalize(x->sc, x->cs, x->cm, x->n_cases, s));
@@ -369,7 +373,8 @@ aqua_create(const aqua_params* params, uint32_t capacity,
         return AQUA_ERR_CUDA;
     }
     // persistent sweep: up to 8 resident blocks per SM fetch chunks
-    x->sweep_grid = (unsigned)(sms > 0 ? sms : 1) * 8u;
+    x->sms = sms > 0 ? sms : 1;
+    x->sweep_grid = (unsigned)x->sms * 8u;
     x->pool_bytes = layout(x, nullptr);
     if (cudaMalloc(&x->pool, x->pool_bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -439,6 +444,18 @@ aqua_set_precision(aqua_ctx* x, int mode)
     if (!x || (mode != AQUA_PRECISION_EXACT && mode != AQUA_PRECISION_FAST))
         return AQUA_ERR_INVALID;
     x->fast = (mode == AQUA_PRECISION_FAST) ? 1 : 0;
+    drop_graphs(x);
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_set_tuning(aqua_ctx* x, uint32_t sweep_variant, uint32_t blocks_per_sm)
+{
+    if (!x || sweep_variant >= (uint32_t)kSweepVariants || blocks_per_sm == 0 ||
+        blocks_per_sm > 32)
+        return AQUA_ERR_INVALID;
+    x->sweep_variant = (int)sweep_variant;
+    x->sweep_grid = (unsigned)x->sms * blocks_per_sm;
     drop_graphs(x);
     return AQUA_OK;
 }

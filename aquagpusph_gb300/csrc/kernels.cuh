@@ -8,8 +8,15 @@ namespace aqua {
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
-constexpr int kSweepThreads = 128;
-constexpr int kSweepQueue = 128;   // queued neighbours per thread (power of 2)
+// sweep variants: 0 = (128 threads, queue 128), 1 = (64, 128),
+// 2 = (128, 64), 3 = (256, 64); threads per block x queued neighbours per
+// thread (the staging depth)
+constexpr int kSweepVariants = 4;
+inline int
+sweep_variant_threads(int v)
+{
+    return v == 1 ? 64 : (v == 3 ? 256 : 128);
+}
 
 // The reference's vec type: float4 in 3-D, float2 in 2-D
 template<int D>
@@ -103,7 +110,7 @@ cudaError_t launch_gather(bool fast, const Consts& c, const StepArgs& a,
                           cudaStream_t s);
 template<int D>
 cudaError_t launch_sweep(bool fast, const Consts& c, const StepArgs& a,
-                         unsigned grid, cudaStream_t s);
+                         unsigned grid, int variant, cudaStream_t s);
 cudaError_t launch_finalize(DevScalars* sc, CaseScalars* cs,
                             const CaseMotion* cm, uint32_t n_cases,
                             cudaStream_t s);
@@ -120,14 +127,14 @@ template<int D>
 cudaError_t launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
 template<int D>
 cudaError_t launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
-                              cudaStream_t s);
+                              int variant, cudaStream_t s);
 }  // namespace exact
 namespace fast {
 template<int D>
 cudaError_t launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
 template<int D>
 cudaError_t launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
-                              cudaStream_t s);
+                              int variant, cudaStream_t s);
 }  // namespace fast
 
 }  // namespace aqua

@@ -193,7 +193,7 @@ launch_gather(bool fast, const Consts& c, const StepArgs& a, cudaStream_t s)
 template<int D>
 cudaError_t
 launch_sweep(bool fast, const Consts& c, const StepArgs& a, unsigned grid,
-             cudaStream_t s)
+             int variant, cudaStream_t s)
 {
     if (a.N) {
         k_chunks<<<(a.N + 255) / 256, 256, 0, s>>>(a.skeys, a.b.cells, a.N,
@@ -202,8 +202,8 @@ launch_sweep(bool fast, const Consts& c, const StepArgs& a, unsigned grid,
         if (e != cudaSuccess)
             return e;
     }
-    return fast ? fast::launch_sweep_impl<D>(c, a, grid, s)
-                : exact::launch_sweep_impl<D>(c, a, grid, s);
+    return fast ? fast::launch_sweep_impl<D>(c, a, grid, variant, s)
+                : exact::launch_sweep_impl<D>(c, a, grid, variant, s);
 }
 
 cudaError_t
@@ -248,8 +248,8 @@ template cudaError_t launch_motion<3>(const StepArgs&, cudaStream_t);
 template cudaError_t launch_gather<2>(bool, const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_gather<3>(bool, const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_sweep<2>(bool, const Consts&, const StepArgs&, unsigned,
-                                     cudaStream_t);
+                                     int, cudaStream_t);
 template cudaError_t launch_sweep<3>(bool, const Consts&, const StepArgs&, unsigned,
-                                     cudaStream_t);
+                                     int, cudaStream_t);
 
 }  // namespace aqua

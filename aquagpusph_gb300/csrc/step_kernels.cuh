@@ -281,7 +281,7 @@ k_gather(Consts c, StepArgs a)
 // holds the first sorted index of the 3^D neighbour cells of the warp's
 // cell.  The scan checks the queues every 32 candidates, where they have
 // room for at least 32 more, so a queue never overflows.
-template<int D>
+template<int D, int NT, int NQ>
 __device__ __forceinline__ float
 sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                uint16_t* queue, uint32_t* cstart)
@@ -323,7 +323,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         float4 pn, vn;
         float2 mn;
         auto fetch = [&](uint32_t h) {
-            const uint32_t e = queue[(h & (kSweepQueue - 1)) * kSweepThreads];
+            const uint32_t e = queue[(h & (NQ - 1)) * NT];
             jn = cstart[e >> 11] + (e & 2047u);
             pn = a.b.posq[jn];
             vn = a.b.velq[jn];
@@ -411,12 +411,12 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         for (uint32_t g = 0; g < count; g += 32) {
             // warp-uniform checkpoint: make room for the next 32 candidates,
             // first draining the entries every lane has (full warps)
-            if (__any_sync(0xffffffffu, qt - qh > kSweepQueue - 32)) {
+            if (__any_sync(0xffffffffu, qt - qh > NQ - 32)) {
                 const uint32_t fill = qt - qh;
                 const uint32_t common = __reduce_min_sync(
                     0xffffffffu, want_shep ? fill : 0xffffffffu);
                 drain(qh + min(common, fill));
-                if (__any_sync(0xffffffffu, qt - qh > kSweepQueue - 32))
+                if (__any_sync(0xffffffffu, qt - qh > NQ - 32))
                     drain(qt);
             }
             const uint32_t gend = min(g + 32u, count);
@@ -443,7 +443,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                                       (jm == 1 || (fluid && jm == -3)) &&
                                       rr < c.q2_reject;
                     if (take) {
-                        queue[(qt & (kSweepQueue - 1)) * kSweepThreads] =
+                        queue[(qt & (NQ - 1)) * NT] =
                             (uint16_t)(((uint32_t)k << 11) | (o + u));
                         qt++;
                     }
@@ -629,12 +629,13 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
 }
 
 // Persistent sweep: warps fetch cell-aligned chunks of <= 32 particles
-template<int D>
-__global__ void __launch_bounds__(kSweepThreads, 5)
+// NT threads per block, NQ queued neighbours per thread (power of 2, >= 64)
+template<int D, int NT, int NQ>
+__global__ void __launch_bounds__(NT, 640 / NT)
 k_sweep(Consts c, StepArgs a)
 {
-    __shared__ uint16_t s_queue[kSweepQueue * kSweepThreads];
-    __shared__ uint32_t s_cstart[kSweepThreads / 32][32];
+    __shared__ uint16_t s_queue[NQ * NT];
+    __shared__ uint32_t s_cstart[NT / 32][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // running minimum of dt_var of the warp's current case, flushed to the
     // case's dt_next when the case changes and at the end
@@ -659,7 +660,7 @@ k_sweep(Consts c, StepArgs a)
                 break;
             const uint2 cw = a.b.chunks[ch];
             const bool valid = (uint32_t)lane < cw.y;
-            float v = sweep_particle<D>(c, a, valid ? cw.x + lane : cw.x, valid,
+            float v = sweep_particle<D, NT, NQ>(c, a, valid ? cw.x + lane : cw.x, valid,
                                         s_queue + threadIdx.x, s_cstart[warp]);
             __syncwarp();  // s_cstart is rewritten for the next chunk
             for (int o = 16; o > 0; o >>= 1)
@@ -686,20 +687,34 @@ launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// sweep variants the tuner chooses from: (threads per block, queue depth)
 template<int D>
 cudaError_t
 launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
-                  cudaStream_t s)
+                  int variant, cudaStream_t s)
 {
     if (a.N == 0)
         return cudaSuccess;
-    k_sweep<D><<<grid, kSweepThreads, 0, s>>>(c, a);
+    switch (variant) {
+    case 1:
+        k_sweep<D, 64, 128><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 2:
+        k_sweep<D, 128, 64><<<grid, 128, 0, s>>>(c, a);
+        break;
+    case 3:
+        k_sweep<D, 256, 64><<<grid, 256, 0, s>>>(c, a);
+        break;
+    default:
+        k_sweep<D, 128, 128><<<grid, 128, 0, s>>>(c, a);
+        break;
+    }
     return cudaGetLastError();
 }
 
 template cudaError_t launch_gather_impl<2>(const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_gather_impl<3>(const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_sweep_impl<2>(const Consts&, const StepArgs&, unsigned,
-                                          cudaStream_t);
+                                          int, cudaStream_t);
 template cudaError_t launch_sweep_impl<3>(const Consts&, const StepArgs&, unsigned,
-                                          cudaStream_t);
+                                          int, cudaStream_t);

@@ -62,6 +62,12 @@ class Solver:
         _lib.check("aqua_set_precision",
                    self.lib.aqua_set_precision(self.ctx, mode))
 
+    def set_tuning(self, sweep_variant: int, blocks_per_sm: int):
+        """Launch shape of the sweep (results do not depend on it)."""
+        _lib.check("aqua_set_tuning", self.lib.aqua_set_tuning(
+            self.ctx, int(sweep_variant), int(blocks_per_sm)))
+        self.tuning = (int(sweep_variant), int(blocks_per_sm))
+
     def set_params(self, params: Params):
         self.params = params
         self._pstruct, self._pkeep = _lib.params_struct(params)
@@ -105,6 +111,10 @@ class Solver:
         """Loads a :class:`aquagpusph_gb300.case.Batch`: its concatenated
         particles, then the split into independent cases (aqua_set_cases)."""
         self.set_case(batch.case, stream)
+        self.set_cases(batch, stream)
+
+    def set_cases(self, batch, stream=None):
+        """The case split of a Batch whose particles are already resident."""
         n = len(batch.offsets) - 1
         offs = np.ascontiguousarray(batch.offsets, np.uint32)
         arr = (_lib.AquaCase * n)()

@@ -49,8 +49,19 @@ STEP_BYTES_2D = 19 * 8 + 96 + 20 * 2
 SWEEP_BYTES_2D = 9 * 8 + 28
 
 
+BATCH = {}
+
+
 def workload(name):
     from aquagpusph_gb300 import case as cases
+    if name == "c2":
+        b = cases.sloshing_batch_2d()
+        BATCH["c2"] = b
+        return b.case, ("batched 2-D sloshing: 64 closed tanks 0.9x0.5 m, fill "
+                        "U[0.1,0.4] m (numpy default_rng(2026)), dx=0.004 m, "
+                        "h=0.008 m, c0=25, BIe walls, roll about the bottom "
+                        "centre with amplitude U[2,8] deg and period U[1.2,2] s, "
+                        f"one probe per tank: N={b.case.N}")
     if name == "c1s":
         c, _ = cpu_sample("c1")
         return c, ("3-D dam break slab at dx=0.005 m, h=0.01 m (tank "
@@ -79,6 +90,10 @@ def cpu_sample(name):
     """A bounded sample of the workload for the CPU runs: the same lattice,
     smoothing length, constants and wall treatment on a smaller tank."""
     from aquagpusph_gb300 import case as cases
+    if name == "c2":
+        b = cases.sloshing_batch_2d(n_cases=8)
+        return b, (f"the first 8 tanks of the batch (N={b.case.N}), each "
+                   "stepped by the oracle in turn")
     if name in ("c1s", "c1m"):
         name = "c1"
     if name == "c0":
@@ -94,16 +109,25 @@ def cpu_sample(name):
 
 
 def time_oracle(c, steps, warmup):
+    """CPU oracle throughput (all host threads) on a case or a batch (its
+    tanks stepped in turn)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     orc = O.load_oracle()
-    st = O.OracleState(c)
     nt = os.cpu_count() or 1
-    orc.step(st, nthreads=nt, steps=max(warmup, 0))
+    if hasattr(c, "cases"):
+        runs = [(O.OracleState(k), m) for k, m in zip(c.cases, c.motions)]
+        n = c.case.N
+    else:
+        runs = [(O.OracleState(c), None)]
+        n = c.N
+    for st, m in runs:
+        orc.step(st, nthreads=nt, steps=max(warmup, 0), motion=m)
     t0 = time.perf_counter()
-    orc.step(st, nthreads=nt, steps=steps)
+    for st, m in runs:
+        orc.step(st, nthreads=nt, steps=steps, motion=m)
     dt = time.perf_counter() - t0
-    return c.N * steps / dt, nt, dt
+    return n * steps / dt, nt, dt
 
 
 class ClockSampler:
@@ -202,6 +226,8 @@ def run_reference(args):
 
 
 def workload_desc(name):
+    if name == "c2":
+        return "batched 2-D sloshing, 64 tanks, dx=0.004 m (N=935,414)"
     if name == "c1m":
         return "3-D dam break, 1.6x0.5x0.6 m tank, dx=0.005 m"
     if name == "c1s":
@@ -222,10 +248,15 @@ def run_ours(args):
     from aquagpusph_gb300.solver import Solver
 
     c, desc = workload(args.workload)
+    batch = BATCH.get(args.workload)
     three_d = c.dims == 3
-    sv = Solver(c.params, capacity=c.N)
+    ncap = (batch.n_cases if batch else 1) * c.params.max_cells()
+    sv = Solver(c.params, capacity=c.N, ihoc_capacity=ncap)
     sv.set_precision(args.precision == "fast")
-    sv.set_case(c)
+    if batch:
+        sv.set_batch(batch)
+    else:
+        sv.set_case(c)
     stream = torch.cuda.Stream()
     sid = stream.cuda_stream
 
@@ -238,6 +269,11 @@ def run_ours(args):
         sv.step(max(args.warmup, 3), graph=True, stream=sid)
     stream.synchronize()
     sv.check(stream=sid)
+    # launch shape of the sweep: timed on this case (cached per GPU/case)
+    tuning = None
+    if not args.no_tune:
+        from aquagpusph_gb300 import autotune
+        tuning = autotune.autotune(sv, args.precision == "fast", stream=sid)
 
     # ---- timed region: K steps replayed from the CUDA graphs
     clocks = ClockSampler(local)
@@ -311,6 +347,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         sv.set_state_raw(c.N, addr_in, True, c.t, c.dt, c.iter, stream=sid)
+        if batch:
+            sv.set_cases(batch, stream=sid)
         sv.step(1, graph=True, stream=sid)
         sv.get_state_raw(addr_out, True, stream=sid)
     stream.synchronize()
@@ -370,6 +408,7 @@ def run_ours(args):
                            "fast" else " (IEEE f32, no FMA contraction; "
                            "bit-exact with the reference kernels)")},
             "other_build": other_line,
+            "tuning": tuning,
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps},
@@ -384,6 +423,13 @@ def run_ours(args):
             "sim": {"t": sc["t"], "dt": sc["dt"], "iter": sc["iter"],
                     "n_cells": [int(x) for x in sc["n_cells"]]},
         }
+        if batch:
+            ks = sv.case_scalars(stream=sid)
+            line["sim"]["cases"] = {
+                "n": len(ks), "t_min": min(k["t"] for k in ks),
+                "t_max": max(k["t"] for k in ks),
+                "dt_min": min(k["dt"] for k in ks),
+                "dt_max": max(k["dt"] for k in ks)}
         print(json.dumps(line), flush=True)
     sv.close()
     if world > 1:
@@ -398,9 +444,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c1s", "c1m"])
+    ap.add_argument("--workload", default="c1",
+                    choices=["c1", "c0", "c1s", "c1m", "c2"])
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--precision", default="fast", choices=["exact", "fast"])
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
