@@ -21,10 +21,22 @@ AQUA_ERR_DT = -3
 AQUA_ERR_CUDA = -4
 AQUA_ERR_NO_MEMORY = -5
 AQUA_ERR_NONFINITE = -6
+AQUA_ERR_IO = -7
+AQUA_ERR_FORMAT = -8
 
 AQUA_PRECISION_EXACT = 0
 AQUA_PRECISION_FAST = 1
 AQUA_NOALLOC_SORT_MAX_KEYS = 1 << 20
+AQUA_REPORT_MAX_VALUES = 1 << 20
+
+# fields of aqua_get_unsorted: name -> (code, vector?)
+FIELDS = {"r": (0, True), "normal": (1, True), "tangent": (2, True),
+          "u": (3, True), "dudt": (4, True), "rho": (5, False),
+          "drhodt": (6, False), "m": (7, False), "p": (8, False),
+          "shepard": (9, False), "imove": (10, False)}
+AQUA_COLUMN_FLOAT = 0
+AQUA_COLUMN_INT = 1
+AQUA_COLUMN_UINT = 2
 
 STATUS_NAMES = {
     AQUA_OK: "AQUA_OK",
@@ -34,6 +46,8 @@ STATUS_NAMES = {
     AQUA_ERR_CUDA: "AQUA_ERR_CUDA",
     AQUA_ERR_NO_MEMORY: "AQUA_ERR_NO_MEMORY",
     AQUA_ERR_NONFINITE: "AQUA_ERR_NONFINITE",
+    AQUA_ERR_IO: "AQUA_ERR_IO",
+    AQUA_ERR_FORMAT: "AQUA_ERR_FORMAT",
 }
 
 _F = C.POINTER(C.c_float)
@@ -131,6 +145,14 @@ SIGNATURES = [
     ("aqua_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("aqua_stage_times", C.c_int, [C.c_void_p, _F, C.c_uint32]),
     ("aqua_launches_per_step", C.c_uint32, [C.c_void_p]),
+    ("aqua_get_unsorted", C.c_int, [C.c_void_p, C.c_int, C.c_uint32,
+                                    C.c_uint32, C.c_void_p, C.c_int,
+                                    C.c_void_p]),
+    ("aqua_free_surface", C.c_int, [C.c_void_p, _F, C.c_uint32, C.c_float,
+                                    C.c_int32, _F, C.c_void_p]),
+    ("aqua_read_fastascii", C.c_int, [C.c_char_p, C.c_uint32, _I, C.c_void_p,
+                                      C.c_uint64, C.POINTER(C.c_uint64),
+                                      C.POINTER(C.c_uint64)]),
 ]
 
 _lib = None

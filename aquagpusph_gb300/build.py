@@ -21,7 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libaqua_gb300.so")
-SOURCES = ("linklist.cu", "step.cu", "step_fast.cu", "api.cu", "noalloc.cu")
+SOURCES = ("linklist.cu", "step.cu", "step_fast.cu", "api.cu", "noalloc.cu",
+           "output.cu", "fastascii.cpp")
 # per-file arithmetic: the fast step kernels trade the reference's exact
 # rounding for FMA contraction and approximate division / square root
 FAST_MATH = {"step_fast.cu"}
@@ -61,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(objdir, src.replace(".cu", ".o"))
+        o = os.path.join(objdir, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([cc] + _flags(src) + ["-c", s, "-o", o])

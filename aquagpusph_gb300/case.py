@@ -195,10 +195,12 @@ def _fill_case(params, parts):
 def dam_break_2d(dx: float = 0.01, tank=(3.22, 1.8), column=(1.2, 0.6),
                  c0: float = 45.0, probe_y: float = 0.16, top: bool = True,
                  refd: float = 998.0, nu: float = 1.0e-6, delta: float = 0.1,
-                 g: float = 9.81, hfac: float = 2.0) -> Case:
+                 g: float = 9.81, hfac: float = 2.0,
+                 extra_probes=()) -> Case:
     """2-D dam break: a water column at the left wall of a closed tank,
     boundary-integral walls at spacing dx, one pressure probe on the right
-    wall (pattern of examples/2D/lobovsky_etal_2014/src/Create.py)."""
+    wall (pattern of examples/2D/lobovsky_etal_2014/src/Create.py), plus
+    optional probes at the (x, y) points of ``extra_probes`` (after it)."""
     L, Ht = tank
     nx = int(round(column[0] / dx))
     ny = int(round(column[1] / dx))
@@ -228,9 +230,10 @@ def dam_break_2d(dx: float = 0.01, tank=(3.22, 1.8), column=(1.2, 0.6),
                           rho=np.full(k, refd), m=np.full(k, dx),
                           p=np.zeros(k), imove=np.full(k, WALL),
                           iset=np.ones(k)))
-    parts.append(dict(r=np.array([[nL * dx, probe_y]]), rho=np.array([refd]),
-                      m=np.array([0.0]), p=np.array([0.0]),
-                      imove=np.array([SENSOR]), iset=np.ones(1)))
+    probes = np.array([[nL * dx, probe_y]] + [list(q) for q in extra_probes])
+    k = len(probes)
+    parts.append(dict(r=probes, rho=np.full(k, refd), m=np.zeros(k),
+                      p=np.zeros(k), imove=np.full(k, SENSOR), iset=np.ones(k)))
     margin = 4 * hfac * dx
     params = Params(dims=2, h=hfac * dx, cs=c0, g=(0.0, -g, 0.0, 0.0),
                     refd=(refd, refd), visc_dyn=(nu * refd, nu * refd),

@@ -41,6 +41,9 @@ struct aqua_ctx
     uint32_t n_cases = 1;
     int has_motion = 0;
     uint32_t* ihoc_out = nullptr;  // ihoc export buffer (ncap)
+    float* report = nullptr;       // report staging (kReportValues)
+    int* fs_keys = nullptr;        // free-surface maxima (kMaxFsSensors)
+    float* fs_out = nullptr;       // decoded free-surface elevations
     int extras = 0;
     int fast = 0;              // 1: -use_fast_math step kernels
     unsigned sweep_grid = 0;   // persistent sweep blocks
@@ -211,6 +214,9 @@ layout(aqua_ctx* x, char* base)
     x->cm = cv.take<CaseMotion>(kMaxCases);
     x->offsets = cv.take<uint32_t>(kMaxCases + 1);
     x->ihoc_out = cv.take<uint32_t>(x->ncap);
+    x->report = cv.take<float>(kReportValues);
+    x->fs_keys = cv.take<int>(kMaxFsSensors);
+    x->fs_out = cv.take<float>(kMaxFsSensors);
     return cv.off + 256;
 }
 
@@ -562,6 +568,71 @@ aqua_get_extra(aqua_ctx* x, aqua_extra* e, int on_host, void* stream)
     AQ_TRY(copy_out(e->lap_p, b.lap_p, N * 4, on_host, s));
     AQ_TRY(copy_out(e->grad_w_bi, b.grad_w_bi, N * VS * 4, on_host, s));
     AQ_TRY(copy_out(e->div_u_bi, b.div_u_bi, N * 4, on_host, s));
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_get_unsorted(aqua_ctx* x, int field, uint32_t first, uint32_t n,
+                  void* out, int on_host, void* stream)
+{
+    if (!x || !out || n == 0 || x->N == 0 || first > x->N || n > x->N - first)
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t VS = (x->dims == 3) ? 4 : 2;
+    const VarSet& d = x->set[x->cur];
+    const float* src = nullptr;
+    uint32_t nc = 1;
+    switch (field) {
+    case AQUA_FIELD_R: src = d.r; nc = VS; break;
+    case AQUA_FIELD_NORMAL: src = d.normal; nc = VS; break;
+    case AQUA_FIELD_TANGENT: src = d.tangent; nc = VS; break;
+    case AQUA_FIELD_U: src = d.u; nc = VS; break;
+    case AQUA_FIELD_DUDT: src = d.dudt; nc = VS; break;
+    case AQUA_FIELD_RHO: src = d.rho; break;
+    case AQUA_FIELD_DRHODT: src = d.drhodt; break;
+    case AQUA_FIELD_M: src = d.m; break;
+    case AQUA_FIELD_P: src = d.p; break;
+    case AQUA_FIELD_SHEPARD: src = x->b.shepard; break;
+    case AQUA_FIELD_IMOVE: break;
+    default: return AQUA_ERR_INVALID;
+    }
+    const size_t values = (size_t)n * nc;
+    if (on_host && values > kReportValues)
+        return AQUA_ERR_CAPACITY;
+    float* dst = on_host ? x->report : (float*)out;
+    if (field == AQUA_FIELD_IMOVE)
+        AQ_CUDA(launch_unsorted_int(d.id, d.imove, x->N, first, n, dst, s));
+    else
+        AQ_CUDA(launch_unsorted(d.id, src, nc, x->N, first, n, dst, s));
+    if (on_host) {
+        AQ_CUDA(cudaMemcpyAsync(out, x->report, values * 4,
+                                cudaMemcpyDeviceToHost, s));
+        AQ_CUDA(cudaStreamSynchronize(s));
+    }
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_free_surface(aqua_ctx* x, const float* sensors, uint32_t n_sensors,
+                  float dr, int32_t case_index, float* out, void* stream)
+{
+    if (!x || !sensors || !out || n_sensors == 0 ||
+        n_sensors > kMaxFsSensors || x->N == 0 || !(dr > 0.f) ||
+        (case_index >= 0 && (uint32_t)case_index >= x->n_cases))
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    FreeSurfaceSensors fs;
+    std::memset(&fs, 0, sizeof(fs));
+    for (uint32_t k = 0; k < n_sensors; k++) {
+        fs.xy[k][0] = sensors[2 * k];
+        fs.xy[k][1] = sensors[2 * k + 1];
+    }
+    const VarSet& d = x->set[x->cur];
+    AQ_CUDA(launch_free_surface(x->dims, d.r, d.imove, d.cid, case_index, x->N,
+                                fs, n_sensors, dr, x->fs_keys, x->fs_out, s));
+    AQ_CUDA(cudaMemcpyAsync(out, x->fs_out, n_sensors * 4ull,
+                            cudaMemcpyDeviceToHost, s));
+    AQ_CUDA(cudaStreamSynchronize(s));
     return AQUA_OK;
 }
 

@@ -122,6 +122,25 @@ cudaError_t launch_export_ihoc(const uint2* cells, uint32_t* ihoc,
                                uint32_t ncap, const DevScalars* sc,
                                cudaStream_t s);
 
+// output.cu: report values in original particle order, free-surface sensors
+constexpr uint32_t kMaxFsSensors = 64;
+constexpr uint32_t kReportValues = AQUA_REPORT_MAX_VALUES;  // report staging
+struct FreeSurfaceSensors
+{
+    float xy[kMaxFsSensors][2];
+};
+cudaError_t launch_unsorted(const uint32_t* id, const float* src, uint32_t nc,
+                            uint32_t N, uint32_t first, uint32_t n, float* out,
+                            cudaStream_t s);
+cudaError_t launch_unsorted_int(const uint32_t* id, const int32_t* src,
+                                uint32_t N, uint32_t first, uint32_t n,
+                                float* out, cudaStream_t s);
+cudaError_t launch_free_surface(int dims, const float* r, const int32_t* imove,
+                                const uint32_t* cid, int32_t case_index,
+                                uint32_t N, const FreeSurfaceSensors& sensors,
+                                uint32_t n_sensors, float dr, int* keys,
+                                float* out, cudaStream_t s);
+
 namespace exact {
 template<int D>
 cudaError_t launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s);

@@ -228,3 +228,30 @@ class Solver:
 
     def launches_per_step(self) -> int:
         return int(self.lib.aqua_launches_per_step(self.ctx))
+
+    def get_unsorted(self, field: str, first: int, n: int, stream=None):
+        """Values of ``field`` for the particles of original index
+        [first, first + n), in original order (host array, synchronises):
+        shape (n,) for scalars, (n, 2|4) for vec fields."""
+        code, is_vec = _lib.FIELDS[field]
+        nc = (4 if self.params.dims == 3 else 2) if is_vec else 1
+        out = np.empty((n, nc), np.int32 if field == "imove" else np.float32)
+        _lib.check("aqua_get_unsorted", self.lib.aqua_get_unsorted(
+            self.ctx, code, int(first), int(n), out.ctypes.data_as(C.c_void_p),
+            1, C.c_void_p(stream or 0)))
+        return out if is_vec else out[:, 0]
+
+    def free_surface(self, sensors, dr: float, case_index: int = -1,
+                     stream=None) -> np.ndarray:
+        """Free-surface elevation at each sensor: ``sensors`` is a list of
+        horizontal positions (x in 2-D, (x, y) in 3-D)."""
+        xy = np.zeros((len(sensors), 2), np.float32)
+        for k, s in enumerate(sensors):
+            s = np.atleast_1d(np.asarray(s, np.float32))
+            xy[k, :len(s)] = s[:2]
+        out = np.empty(len(sensors), np.float32)
+        _lib.check("aqua_free_surface", self.lib.aqua_free_surface(
+            self.ctx, xy.ctypes.data_as(_lib._F), len(sensors), float(dr),
+            int(case_index), out.ctypes.data_as(_lib._F),
+            C.c_void_p(stream or 0)))
+        return out

@@ -91,8 +91,8 @@ def cpu_sample(name):
     smoothing length, constants and wall treatment on a smaller tank."""
     from aquagpusph_gb300 import case as cases
     if name == "c2":
-        b = cases.sloshing_batch_2d(n_cases=8)
-        return b, (f"the first 8 tanks of the batch (N={b.case.N}), each "
+        b = cases.sloshing_batch_2d()
+        return b, (f"the whole batch (64 tanks, N={b.case.N}), each tank "
                    "stepped by the oracle in turn")
     if name in ("c1s", "c1m"):
         name = "c1"
@@ -108,9 +108,11 @@ def cpu_sample(name):
     return c, desc
 
 
-def time_oracle(c, steps, warmup):
+def time_oracle(c, steps, warmup, min_seconds=0.0, max_steps=100000):
     """CPU oracle throughput (all host threads) on a case or a batch (its
-    tanks stepped in turn)."""
+    tanks stepped in turn): ``steps`` steps, repeated until ``min_seconds``
+    of CPU work have passed.  Returns (particle-steps/s, threads, seconds,
+    steps)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     orc = O.load_oracle()
@@ -123,11 +125,16 @@ def time_oracle(c, steps, warmup):
         n = c.N
     for st, m in runs:
         orc.step(st, nthreads=nt, steps=max(warmup, 0), motion=m)
+    done = 0
     t0 = time.perf_counter()
-    for st, m in runs:
-        orc.step(st, nthreads=nt, steps=steps, motion=m)
-    dt = time.perf_counter() - t0
-    return n * steps / dt, nt, dt
+    while True:
+        for st, m in runs:
+            orc.step(st, nthreads=nt, steps=steps, motion=m)
+        done += steps
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds or done >= max_steps:
+            break
+    return n * done / dt, nt, dt, done
 
 
 class ClockSampler:
@@ -206,7 +213,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     c, desc = cpu_sample(args.workload)
-    value, nt, secs = time_oracle(c, args.steps, args.warmup)
+    value, nt, secs, _ = time_oracle(c, args.steps, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -388,9 +395,10 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu_baseline:
             cs, sdesc = cpu_sample(args.workload)
-            v, nt, secs = time_oracle(cs, args.cpu_steps, 1)
+            v, nt, secs, done = time_oracle(cs, args.cpu_steps, 1,
+                                            min_seconds=args.cpu_seconds)
             cpu = {"value": v, "unit": UNIT, "cores": nt, "kind": "port",
-                   "sample": f"{sdesc}, {args.cpu_steps} steps in {secs:.1f} s "
+                   "sample": f"{sdesc}, {done} steps in {secs:.1f} s "
                              "(CPU oracle: C++ restatement of the reference "
                              "kernels, OpenMP over particles)"}
         line = {
@@ -449,6 +457,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--precision", default="fast", choices=["exact", "fast"])
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="minimum CPU work of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

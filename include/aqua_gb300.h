@@ -46,7 +46,9 @@ typedef enum
     AQUA_ERR_DT = -3,          /* time step not > 0 (variableTimeStep.xml:16) */
     AQUA_ERR_CUDA = -4,        /* a CUDA runtime call failed */
     AQUA_ERR_NO_MEMORY = -5,   /* device allocation failed */
-    AQUA_ERR_NONFINITE = -6    /* non-finite position reached the link-list */
+    AQUA_ERR_NONFINITE = -6,   /* non-finite position reached the link-list */
+    AQUA_ERR_IO = -7,          /* a file could not be opened or read */
+    AQUA_ERR_FORMAT = -8       /* a particles file line is malformed */
 } aqua_status;
 
 /* Scalar Variables and Definitions of one case.  The Definitions are the
@@ -281,6 +283,66 @@ aqua_status aqua_stage_times(aqua_ctx* ctx, float* ms, uint32_t n);
 aqua_status aqua_radix_sort_noalloc(uint32_t* keys, uint32_t* perm,
                                     uint32_t* inv_perm, uint32_t n,
                                     uint32_t key_bits, void* stream);
+
+/* Fields of the resident state for aqua_get_unsorted(). */
+#define AQUA_FIELD_R 0        /* vec */
+#define AQUA_FIELD_NORMAL 1   /* vec */
+#define AQUA_FIELD_TANGENT 2  /* vec */
+#define AQUA_FIELD_U 3        /* vec */
+#define AQUA_FIELD_DUDT 4     /* vec */
+#define AQUA_FIELD_RHO 5
+#define AQUA_FIELD_DRHODT 6
+#define AQUA_FIELD_M 7
+#define AQUA_FIELD_P 8
+#define AQUA_FIELD_SHEPARD 9
+#define AQUA_FIELD_IMOVE 10   /* int32 values */
+/* Report staging limit of aqua_get_unsorted() into host memory (values) */
+#define AQUA_REPORT_MAX_VALUES (1u << 20)
+
+/* The values of one field for the particles whose original index (the id
+ * given at aqua_set_state) lies in [first, first + n), in original order:
+ * out[(id - first) * nc + k], nc = components of the field (2 or 4 for vec,
+ * else 1), 32-bit values.  The reference's particle reports read their
+ * fields this way (CalcServer::getUnsortedMem, used by SetTabFile.cpp:
+ * 282-287).  `on_host` = 1: out is host memory, n * nc <=
+ * AQUA_REPORT_MAX_VALUES (else AQUA_ERR_CAPACITY), and the call synchronises
+ * `stream`; 0: out is device memory and the call only enqueues. */
+aqua_status aqua_get_unsorted(aqua_ctx* ctx, int field, uint32_t first,
+                              uint32_t n, void* out, int on_host,
+                              void* stream);
+
+/* Free-surface elevation sensors, as the wave-height sensors of the 3-D
+ * dam-break example (examples/3D/spheric_testcase2_dambreak/src/templates/
+ * h_sensor.cl:37-61 and the max reductions of Sensors.xml:43-62): for
+ * sensor k at horizontal position sensors[2k], sensors[2k+1] (x, y; y unused
+ * in 2-D), out[k] = max over particles of h_i, where h_i = r_i[up] + dr/2
+ * for fluid particles (imove > 0) with |x_i - x_k| <= 2 dr (and |y_i - y_k|
+ * <= 2 dr in 3-D) and 0 for every other particle; up = y in 2-D, z in 3-D.
+ * case_index >= 0 restricts the maximum to that case of a batch (-1: all
+ * particles).  At most 64 sensors; out is host memory; synchronises. */
+aqua_status aqua_free_surface(aqua_ctx* ctx, const float* sensors,
+                              uint32_t n_sensors, float dr, int32_t case_index,
+                              float* out, void* stream);
+
+/* Column types of aqua_read_fastascii() */
+#define AQUA_COLUMN_FLOAT 0   /* float and vec fields */
+#define AQUA_COLUMN_INT 1     /* int fields (imove) */
+#define AQUA_COLUMN_UINT 2    /* unsigned int fields */
+
+/* Reads a FastASCII particles file (InputOutput/FastASCII.cpp and the line
+ * rules of InputOutput/ASCII.cpp:65-240, 374-403): comments from '#', the
+ * separators " ;()[]{}\t," (runs count once), one particle per non-empty
+ * line with exactly n_cols numbers of the given column types.  Host only, no
+ * GPU.  out = NULL: *n_rows = number of particle lines (no parsing).
+ * Otherwise the numbers go to out as 32-bit words, row-major
+ * (n_rows x n_cols, at most max_rows rows, else AQUA_ERR_CAPACITY).
+ * AQUA_ERR_IO: the file cannot be read.  AQUA_ERR_FORMAT: a line with
+ * another number of fields, or a column with no number or out of its type's
+ * range; *bad_line (if not NULL) = its 1-based line number. */
+aqua_status aqua_read_fastascii(const char* path, uint32_t n_cols,
+                                const int32_t* col_types, void* out,
+                                uint64_t max_rows, uint64_t* n_rows,
+                                uint64_t* bad_line);
 
 /* Number of kernel launches one aqua_step() step issues (for accounting). */
 uint32_t aqua_launches_per_step(aqua_ctx* ctx);

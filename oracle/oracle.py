@@ -223,3 +223,36 @@ def build_oracle(ref=False):
     import subprocess
     targets = ["all"] + (["ref"] if ref else [])
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+def free_surface(st: OracleState, sensors, dr: float, dims: int):
+    """Wave-height sensors restated on the oracle's state
+    (examples/3D/spheric_testcase2_dambreak/src/templates/h_sensor.cl:37-61
+    and the max reductions of Sensors.xml:43-62): h_i = r_i[up] + dr/2 for
+    fluid particles within 2 dr of the sensor horizontally, 0 otherwise;
+    H = max_i h_i.  ``sensors``: x (2-D) or (x, y) (3-D) per sensor."""
+    r = st["r"]
+    fluid = st["imove"] > 0
+    dr = np.float32(dr)
+    two = np.float32(2.0) * dr
+    out = []
+    for s in sensors:
+        s = np.atleast_1d(np.asarray(s, np.float32))
+        far = np.abs(r[:, 0] - s[0]) > two
+        if dims == 3:
+            far |= np.abs(r[:, 1] - s[1]) > two
+        h = np.where(fluid & ~far, r[:, dims - 1] + np.float32(0.5) * dr,
+                     np.float32(0.0)).astype(np.float32)
+        out.append(np.float32(h.max()) if len(h) else np.float32(-np.inf))
+    return np.array(out, np.float32)
+
+
+def probe_values(st: OracleState, field: str, first: int, n: int):
+    """Values of ``field`` for the particles of original index
+    [first, first + n), in original order (the oracle keeps its state sorted
+    by cell, like the reference)."""
+    pos = np.empty(n, np.int64)
+    ids = st["id"]
+    sel = np.nonzero((ids >= first) & (ids < first + n))[0]
+    pos[ids[sel] - first] = sel
+    return st[field][pos]
