@@ -9,10 +9,11 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "aqua_gb300.h")
+LEARNED_HEADER = os.path.join(ROOT, "include", "aqua_learned.h")
 
 
-def declared_functions():
-    text = open(HEADER).read()
+def declared_functions(header=HEADER):
+    text = open(header).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"^\s*(?:const\s+)?[\w*]+\s+\**(aqua_\w+)\s*\(",
                                  text, flags=re.M)))
@@ -58,3 +59,13 @@ def test_structs_match_between_oracle_and_library():
     assert [f[0] for f in O.AqParams._fields_][: len(lib_fields)] == lib_fields
     for name in lib_fields:
         assert getattr(O.AqParams, name).offset == getattr(_lib.AquaParams, name).offset
+
+
+def test_learned_header_exported_and_bound(lib_path):
+    from aquagpusph_gb300 import learned
+    names = declared_functions(LEARNED_HEADER)
+    assert len(names) >= 20
+    lib = ctypes.CDLL(lib_path)
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(learned.SIGNATURES) == set(names)
