@@ -51,7 +51,12 @@ def _p(t):
     return _vp(t.data_ptr()) if t is not None else _vp(0)
 
 
+# entry points called (each launches at least one kernel); for accounting
+CALLS = [0]
+
+
 def _chk(name, st):
+    CALLS[0] += 1
     _lib.check(name, st)
 
 

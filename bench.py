@@ -90,7 +90,7 @@ def cpu_sample(name):
     """A bounded sample of the workload for the CPU runs: the same lattice,
     smoothing length, constants and wall treatment on a smaller tank."""
     from aquagpusph_gb300 import case as cases
-    if name == "c2":
+    if name in ("c2", "c3"):
         b = cases.sloshing_batch_2d()
         return b, (f"the whole batch (64 tanks, N={b.case.N}), each tank "
                    "stepped by the oracle in turn")
@@ -233,7 +233,7 @@ def run_reference(args):
 
 
 def workload_desc(name):
-    if name == "c2":
+    if name in ("c2", "c3"):
         return "batched 2-D sloshing, 64 tanks, dx=0.004 m (N=935,414)"
     if name == "c1m":
         return "3-D dam break, 1.6x0.5x0.6 m tank, dx=0.005 m"
@@ -446,6 +446,178 @@ def run_ours(args):
     return 0
 
 
+def run_learned(args):
+    """Learned k = 8 proposals with a plain judge on a quarter of the cases,
+    on the 64-tank sloshing batch; the network is first trained on plain
+    trajectories of 32 other tanks drawn from the same distribution."""
+    import torch
+    from aquagpusph_gb300 import case as cases
+    from aquagpusph_gb300 import learned as Lm
+    from aquagpusph_gb300.solver import Solver
+    torch.cuda.set_device(0)
+    K = 8
+    t0 = time.perf_counter()
+    tb = cases.sloshing_batch_2d(n_cases=32, seed=1234)
+    pairs, dts = Lm.collect_pairs(tb, K, n_pairs=args.train_pairs, gap=300,
+                                  warm=500)
+    model = Lm.Model(2, seed=0)
+    Lm.fit_scales(model, pairs, dts, K, tb.case.params, Lm.case_ids(tb))
+    sv_t = Solver(tb.case.params, capacity=tb.case.N)
+    tr = Lm.Trainer(model, sv_t, tb, K, lr=1e-3, cases_per_step=16)
+    held = list(range(len(pairs) - 4, len(pairs)))
+
+    def held_loss(m):
+        tr.model = m
+        v = [float(tr.batch_loss(pairs[i], dts[i], 0, 16, train=False)[1].item())
+             for i in held]
+        tr.model = model
+        return float(np.mean(v))
+    zero = Lm.Model(2, seed=0)
+    zero.flat.zero_()
+    zero._refresh()
+    zero.scales.copy_(model.scales)
+    zero.out_scale = model.out_scale
+    loss_zero = held_loss(zero)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.train_iters):
+        tr.step(pairs[:-4], dts[:-4])
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    loss_trained = held_loss(model)
+    sv_t.close()
+    prep_s = time.perf_counter() - t0
+
+    eb = cases.sloshing_batch_2d()
+    c = eb.case
+    sv = Solver(c.params, capacity=c.N,
+                ihoc_capacity=eb.n_cases * c.params.max_cells())
+    sv.set_precision(args.precision == "fast")
+    sv.set_batch(eb)
+    sv.step(args.eval_warm, graph=True)
+    sv.check()
+    run = Lm.ProposalRunner(sv, eb, model, k=K, judge_fraction=0.25, tol=0.02,
+                            fast=args.precision == "fast")
+    for _ in range(args.warmup):
+        run.advance()
+    for key in ("p_err", "rho_err"):
+        run.stats[key] = []
+    run.stats.update(proposals=0, judged=0, rolled_back=0)
+    # forward pass alone (the network's dense layers), CUDA events
+    s0 = Lm.Snapshot.capture(sv, 2)
+    g = Lm.Graph(sv, 2, s0["r"], s0["imove"], run.cid, s0.n, run.radius)
+    x = Lm.Inputs(g, s0["r"], s0["u"], s0["rho"], s0["dudt"], s0["drhodt"],
+                  s0["imove"], s0["normal"])
+    net = Lm.Network(model, g, x)
+    net.forward()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    net.forward()
+    e1.record()
+    e1.synchronize()
+    fwd_ms = e0.elapsed_time(e1)
+    flops = 0
+    for name, n, kk, act in Lm.LAYERS:
+        rows = g.n_edges if name[0] == "e" else g.n_nodes
+        flops += 2 * rows * n * kk
+    del net, x, g, s0
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    calls0 = Lm.CALLS[0]
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    for _ in range(args.steps):
+        run.advance()
+    torch.cuda.synchronize()
+    dt_s = time.perf_counter() - t2
+    clk = clocks.stop()
+    calls = Lm.CALLS[0] - calls0
+    judge_launches = args.steps * K * run.judge.launches_per_step()
+    value = c.N * K * args.steps / dt_s
+    # the plain step on the same batch, same number of particle-steps
+    e0.record()
+    sv.step(K * args.steps, graph=True)
+    e1.record()
+    e1.synchronize()
+    sv.check()
+    plain_ms = e0.elapsed_time(e1)
+    plain_value = c.N * K * args.steps / (plain_ms * 1e-3)
+    # end to end: state from pinned host memory in, proposal, state out
+    host = Lm.Snapshot.capture(sv, 2)
+    pin = {f: torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+           for f, v in host.a.items()}
+    for f in pin:
+        pin[f].copy_(host[f])
+    out = {f: torch.empty_like(v, pin_memory=True) for f, v in pin.items()}
+    scal = sv.case_scalars()
+    n_e2e = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    for _ in range(n_e2e):
+        sv.set_state_raw(c.N, {f: v.data_ptr() for f, v in pin.items()}, True,
+                         scal[0]["t"], scal[0]["dt"], scal[0]["iter"])
+        Lm.ProposalRunner._set_cases(sv, eb, scal)
+        run.advance()
+        sv.get_state_raw({f: v.data_ptr() for f, v in out.items()
+                          if f != "id"}, True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t3
+    nbytes = sum(v.numel() * v.element_size() for v in pin.values())
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("bf16_tflops") or 1900.0
+    st = run.stats
+    line = {
+        "metric": "particle-steps/s (learned k=8 proposal + plain judge on 25% "
+                  "of the cases, 1 GB300)",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 network (f32 accumulate), f32 state", "data": "synthetic",
+        "config": {"workload": workload_desc("c2") + "; one step = one proposal "
+                   f"of k={K} plain steps", "training": {
+                       "tanks": "32 sloshing tanks, seed 1234 (config-2 distribution)",
+                       "pairs": args.train_pairs, "iterations": args.train_iters,
+                       "cases_per_step": 16, "train_s": train_s,
+                       "prep_s": prep_s},
+                   "judge": "plain step re-run of 25% of the cases; rollback at "
+                            "> 2% probe-pressure error (of max(|p|, rho g 4h)) "
+                            "or > 2% density error (of refd)"},
+        "plain_value": plain_value, "learned_over_plain": value / plain_value,
+        "heldout_mse": {"trained": loss_trained,
+                        "extrapolation_only": loss_zero},
+        "judge_stats": {"judged": st["judged"], "rolled_back": st["rolled_back"],
+                        "p_err_median": float(np.median(st["p_err"])),
+                        "p_err_max": float(np.max(st["p_err"])),
+                        "rho_err_median": float(np.median(st["rho_err"])),
+                        "rho_err_max": float(np.max(st["rho_err"]))},
+        "e2e": {"value": c.N * K * n_e2e / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": n_e2e},
+        "gpu_launches": calls + judge_launches,
+        "gpu_launches_note": "library entry points called (each launches at "
+                             "least one kernel) plus the judge's plain-step "
+                             "kernels",
+        "roofline": {"bound": "tensor", "kernel": "network forward (dense "
+                     "layers and graph gathers)", "achieved": flops / (fwd_ms * 1e-3) / 1e12,
+                     "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / (fwd_ms * 1e-3) / 1e12 / peak,
+                     "peak_source": "measured" if peaks.get("bf16_tflops") else "fallback",
+                     "flops_per_forward": flops, "forward_ms": fwd_ms,
+                     "traffic": None},
+        "clocks": clk, "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+    sv.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,7 +625,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c1",
-                    choices=["c1", "c0", "c1s", "c1m", "c2"])
+                    choices=["c1", "c0", "c1s", "c1m", "c2", "c3"])
+    ap.add_argument("--train-pairs", type=int, default=24)
+    ap.add_argument("--train-iters", type=int, default=300)
+    ap.add_argument("--eval-warm", type=int, default=3000)
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--precision", default="fast", choices=["exact", "fast"])
     ap.add_argument("--no-tune", action="store_true")
@@ -465,6 +640,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "c3":
+        return run_learned(args)
     return run_ours(args)
 
 
