@@ -284,7 +284,7 @@ k_gather(Consts c, StepArgs a)
 template<int D, int NT, int NQ>
 __device__ __forceinline__ float
 sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
-               uint16_t* queue, uint32_t* cstart)
+               uint16_t* queue, uint32_t* cstart, float4* grp)
 {
     constexpr int VS = Vec<D>::VS;
     constexpr int NC = (D == 3) ? 27 : 9;
@@ -393,6 +393,21 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         }
     };
 
+    // box of the positions of the lanes that take neighbours (empty when
+    // none does); candidates farther than the support from it are skipped
+    float blo[3], bhi[3];
+    for (int d = 0; d < 3; d++) {
+        blo[d] = want_shep ? ri[d] : INFINITY;
+        bhi[d] = want_shep ? ri[d] : -INFINITY;
+        for (int o = 16; o > 0; o >>= 1) {
+            blo[d] = fminf(blo[d], __shfl_xor_sync(0xffffffffu, blo[d], o));
+            bhi[d] = fmaxf(bhi[d], __shfl_xor_sync(0xffffffffu, bhi[d], o));
+        }
+    }
+    // a margin over the per-lane bound covers rounding differences between
+    // the box distance and the lanes' own distances
+    const float q2_box = c.q2_reject * 1.001f;
+
     // first sorted index of each neighbour cell (same for the whole warp)
     const int lane = threadIdx.x & 31;
     if (lane < NC)
@@ -420,35 +435,56 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                     drain(qt);
             }
             const uint32_t gend = min(g + 32u, count);
-            // four candidates per iteration, loads first
-            for (uint32_t o = g; o < gend; o += 4) {
-                float4 p4[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-                    if (o + u < gend)
-                        p4[u] = a.b.posq[se.x + o + u];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if (o + u >= gend)
-                        break;
-                    const float4 pj = p4[u];
-                    const int jm = __float_as_int(pj.w);
-                    const float d0 = pj.x - ri[0], d1 = pj.y - ri[1];
-                    float rr = d0 * d0 + d1 * d1;
-                    if (D == 3) {
-                        const float d2 = pj.z - ri[2];
-                        rr = rr + d2 * d2;
-                    }
-                    const bool take = want_shep &&
-                                      (jm == 1 || (fluid && jm == -3)) &&
-                                      rr < c.q2_reject;
-                    if (take) {
-                        queue[(qt & (NQ - 1)) * NT] =
-                            (uint16_t)(((uint32_t)k << 11) | (o + u));
-                        qt++;
-                    }
+            // lane-parallel pre-filter of the 32 candidates of this group:
+            // drop those farther than the support from the box of the
+            // chunk's particles (no lane can take them); the survivors are
+            // then tested per lane in their visiting order
+            bool cand = false;
+            if (g + lane < gend) {
+                const float4 pc = a.b.posq[se.x + g + lane];
+                grp[lane] = pc;
+                const int jm = __float_as_int(pc.w);
+                const float bx = fmaxf(fmaxf(blo[0] - pc.x, pc.x - bhi[0]), 0.f);
+                const float by = fmaxf(fmaxf(blo[1] - pc.y, pc.y - bhi[1]), 0.f);
+                float bb = bx * bx + by * by;
+                if (D == 3) {
+                    const float bz = fmaxf(fmaxf(blo[2] - pc.z, pc.z - bhi[2]), 0.f);
+                    bb = bb + bz * bz;
                 }
+                cand = (jm == 1 || jm == -3) && bb < q2_box;
             }
+            uint32_t bal = __ballot_sync(0xffffffffu, cand);
+            __syncwarp();
+            auto consider = [&](const float4 pj, uint32_t off) {
+                const int jm = __float_as_int(pj.w);
+                const float d0 = pj.x - ri[0], d1 = pj.y - ri[1];
+                float rr = d0 * d0 + d1 * d1;
+                if (D == 3) {
+                    const float d2 = pj.z - ri[2];
+                    rr = rr + d2 * d2;
+                }
+                const bool take = want_shep && (jm == 1 || (fluid && jm == -3)) &&
+                                  rr < c.q2_reject;
+                if (take) {
+                    queue[(qt & (NQ - 1)) * NT] = (uint16_t)(((uint32_t)k << 11) | off);
+                    qt++;
+                }
+            };
+            while (bal) {
+                // two survivors per iteration, in visiting order
+                const uint32_t b0 = __ffs(bal) - 1;
+                bal &= bal - 1;
+                const bool two = bal != 0;
+                const uint32_t b1 = two ? (uint32_t)(__ffs(bal) - 1) : b0;
+                if (two)
+                    bal &= bal - 1;
+                const float4 p0 = grp[b0];
+                const float4 p1 = grp[b1];
+                consider(p0, g + b0);
+                if (two)
+                    consider(p1, g + b1);
+            }
+            __syncwarp();  // grp is rewritten by the next group
         }
     }
     drain(qt);
@@ -636,6 +672,7 @@ k_sweep(Consts c, StepArgs a)
 {
     __shared__ uint16_t s_queue[NQ * NT];
     __shared__ uint32_t s_cstart[NT / 32][32];
+    __shared__ float4 s_grp[NT / 32][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // running minimum of dt_var of the warp's current case, flushed to the
     // case's dt_next when the case changes and at the end
@@ -661,7 +698,8 @@ k_sweep(Consts c, StepArgs a)
             const uint2 cw = a.b.chunks[ch];
             const bool valid = (uint32_t)lane < cw.y;
             float v = sweep_particle<D, NT, NQ>(c, a, valid ? cw.x + lane : cw.x, valid,
-                                        s_queue + threadIdx.x, s_cstart[warp]);
+                                        s_queue + threadIdx.x, s_cstart[warp],
+                                        s_grp[warp]);
             __syncwarp();  // s_cstart is rewritten for the next chunk
             for (int o = 16; o > 0; o >>= 1)
                 v = cl_min(v, __shfl_xor_sync(0xffffffffu, v, o));
