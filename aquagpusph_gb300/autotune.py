@@ -19,9 +19,10 @@ from . import _lib
 
 # (variant, threads per block, queued neighbours per thread); the variant
 # numbers are those of aqua_set_tuning
-VARIANTS = ((0, 128, 128), (1, 64, 128), (2, 128, 64), (3, 256, 64))
-BLOCKS_PER_SM = (2, 3, 4, 5, 6, 8, 10)
-MAX_THREADS_PER_SM = 2048
+VARIANTS = ((0, 128, 128), (1, 64, 128), (2, 64, 64), (3, 128, 64))
+# resident warps per SM tried for each variant (blocks = warps * 32 / threads)
+WARPS_PER_SM = (8, 10, 12, 16, 20, 24)
+MAX_BLOCKS_PER_SM = 32
 
 
 def cache_path() -> str:
@@ -74,8 +75,9 @@ def _save(d):
 
 def candidates():
     for v, threads, queue in VARIANTS:
-        for b in BLOCKS_PER_SM:
-            if b * threads <= MAX_THREADS_PER_SM:
+        for w in WARPS_PER_SM:
+            b = w * 32 // threads
+            if b * threads == w * 32 and 1 <= b <= MAX_BLOCKS_PER_SM:
                 yield v, b
 
 

@@ -378,9 +378,9 @@ aqua_create(const aqua_params* params, uint32_t capacity,
         delete x;
         return AQUA_ERR_CUDA;
     }
-    // persistent sweep: up to 8 resident blocks per SM fetch chunks
+    // persistent sweep: 5 blocks of 128 threads per SM fetch chunks
     x->sms = sms > 0 ? sms : 1;
-    x->sweep_grid = (unsigned)x->sms * 8u;
+    x->sweep_grid = (unsigned)x->sms * 5u;
     x->pool_bytes = layout(x, nullptr);
     if (cudaMalloc(&x->pool, x->pool_bytes) != cudaSuccess) {
         cudaGetLastError();

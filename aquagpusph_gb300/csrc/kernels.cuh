@@ -8,14 +8,14 @@ namespace aqua {
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
-// sweep variants: 0 = (128 threads, queue 128), 1 = (64, 128),
-// 2 = (128, 64), 3 = (256, 64); threads per block x queued neighbours per
-// thread (the staging depth)
+// sweep variants: threads per block x queued neighbours per thread (the
+// staging depth) x queue entry: 0 = (128, 128, 16-bit), 1 = (64, 128,
+// 16-bit), 2 = (64, 64, 32-bit), 3 = (128, 64, 32-bit)
 constexpr int kSweepVariants = 4;
 inline int
 sweep_variant_threads(int v)
 {
-    return v == 1 ? 64 : (v == 3 ? 256 : 128);
+    return (v == 1 || v == 2) ? 64 : 128;
 }
 
 // The reference's vec type: float4 in 3-D, float2 in 2-D

@@ -276,15 +276,17 @@ k_gather(Consts c, StepArgs a)
 // 3^D cells in the reference order and appends the ones inside the support
 // to this lane's ring queue in shared memory (one column per thread); the
 // drain pops the queue in order and accumulates.  Every sum keeps the
-// reference's order.  A queue entry is 16 bits: the neighbour-cell slot k
-// (5 bits) and the candidate's offset in that cell (11 bits); `cstart`
-// holds the first sorted index of the 3^D neighbour cells of the warp's
-// cell.  The scan checks the queues every 32 candidates, where they have
-// room for at least 32 more, so a queue never overflows.
-template<int D, int NT, int NQ>
+// reference's order.  A queue entry (QE) is either the neighbour's sorted
+// index (32 bits) or, to halve the queue's shared memory, 16 bits: the
+// neighbour-cell slot k (5 bits) and the candidate's offset in that cell
+// (11 bits), resolved through `cstart`, the first sorted index of the 3^D
+// neighbour cells of the warp's cell.  The scan checks the queues every 32
+// candidates, where they have room for at least 32 more, so a queue never
+// overflows.
+template<int D, int NT, int NQ, typename QE>
 __device__ __forceinline__ float
 sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
-               uint16_t* queue, uint32_t* cstart, float4* grp)
+               QE* queue, uint32_t* cstart, float4* grp)
 {
     constexpr int VS = Vec<D>::VS;
     constexpr int NC = (D == 3) ? 27 : 9;
@@ -324,7 +326,10 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         float2 mn;
         auto fetch = [&](uint32_t h) {
             const uint32_t e = queue[(h & (NQ - 1)) * NT];
-            jn = cstart[e >> 11] + (e & 2047u);
+            if constexpr (sizeof(QE) == 2)
+                jn = cstart[e >> 11] + (e & 2047u);
+            else
+                jn = e;
             pn = a.b.posq[jn];
             vn = a.b.velq[jn];
             mn = a.b.pmq[jn];
@@ -408,16 +413,18 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     // the box distance and the lanes' own distances
     const float q2_box = c.q2_reject * 1.001f;
 
-    // first sorted index of each neighbour cell (same for the whole warp)
     const int lane = threadIdx.x & 31;
-    if (lane < NC)
-        cstart[lane] = a.b.cells[neighbour_cell<D>(key_i, lane, nx, nxy)].x;
-    __syncwarp();
+    if constexpr (sizeof(QE) == 2) {
+        // first sorted index of each neighbour cell (same for the whole warp)
+        if (lane < NC)
+            cstart[lane] = a.b.cells[neighbour_cell<D>(key_i, lane, nx, nxy)].x;
+        __syncwarp();
+    }
     for (int k = 0; k < NC; k++) {
         const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
         const uint2 se = a.b.cells[cn];
         const uint32_t count = se.y - se.x;
-        if (count > 2048u) {
+        if (sizeof(QE) == 2 && count > 2048u) {
             // the 11-bit offsets cannot address such a cell
             if (lane == 0)
                 atomicOr(&a.sc->err, kErrCapacity);
@@ -466,7 +473,10 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                 const bool take = want_shep && (jm == 1 || (fluid && jm == -3)) &&
                                   rr < c.q2_reject;
                 if (take) {
-                    queue[(qt & (NQ - 1)) * NT] = (uint16_t)(((uint32_t)k << 11) | off);
+                    if constexpr (sizeof(QE) == 2)
+                        queue[(qt & (NQ - 1)) * NT] = (QE)(((uint32_t)k << 11) | off);
+                    else
+                        queue[(qt & (NQ - 1)) * NT] = se.x + off;
                     qt++;
                 }
             };
@@ -666,11 +676,12 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
 
 // Persistent sweep: warps fetch cell-aligned chunks of <= 32 particles
 // NT threads per block, NQ queued neighbours per thread (power of 2, >= 64)
-template<int D, int NT, int NQ>
+// of type QE
+template<int D, int NT, int NQ, typename QE>
 __global__ void __launch_bounds__(NT, 640 / NT)
 k_sweep(Consts c, StepArgs a)
 {
-    __shared__ uint16_t s_queue[NQ * NT];
+    __shared__ QE s_queue[NQ * NT];
     __shared__ uint32_t s_cstart[NT / 32][32];
     __shared__ float4 s_grp[NT / 32][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -697,10 +708,10 @@ k_sweep(Consts c, StepArgs a)
                 break;
             const uint2 cw = a.b.chunks[ch];
             const bool valid = (uint32_t)lane < cw.y;
-            float v = sweep_particle<D, NT, NQ>(c, a, valid ? cw.x + lane : cw.x, valid,
-                                        s_queue + threadIdx.x, s_cstart[warp],
-                                        s_grp[warp]);
-            __syncwarp();  // s_cstart is rewritten for the next chunk
+            float v = sweep_particle<D, NT, NQ, QE>(
+                c, a, valid ? cw.x + lane : cw.x, valid, s_queue + threadIdx.x,
+                s_cstart[warp], s_grp[warp]);
+            __syncwarp();  // s_cstart and s_grp are rewritten for the next chunk
             for (int o = 16; o > 0; o >>= 1)
                 v = cl_min(v, __shfl_xor_sync(0xffffffffu, v, o));
             const uint32_t kc = a.dst.cid[cw.x];
@@ -725,7 +736,8 @@ launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
-// sweep variants the tuner chooses from: (threads per block, queue depth)
+// sweep variants the tuner chooses from: (threads per block, queue depth,
+// queue entry type); the static shared memory of a block stays <= 34 KB
 template<int D>
 cudaError_t
 launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
@@ -735,16 +747,16 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
         return cudaSuccess;
     switch (variant) {
     case 1:
-        k_sweep<D, 64, 128><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 128, uint16_t><<<grid, 64, 0, s>>>(c, a);
         break;
     case 2:
-        k_sweep<D, 128, 64><<<grid, 128, 0, s>>>(c, a);
+        k_sweep<D, 64, 64, uint32_t><<<grid, 64, 0, s>>>(c, a);
         break;
     case 3:
-        k_sweep<D, 256, 64><<<grid, 256, 0, s>>>(c, a);
+        k_sweep<D, 128, 64, uint32_t><<<grid, 128, 0, s>>>(c, a);
         break;
     default:
-        k_sweep<D, 128, 128><<<grid, 128, 0, s>>>(c, a);
+        k_sweep<D, 128, 128, uint16_t><<<grid, 128, 0, s>>>(c, a);
         break;
     }
     return cudaGetLastError();

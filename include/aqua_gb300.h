@@ -189,10 +189,11 @@ aqua_status aqua_set_extras(aqua_ctx* ctx, int on);
 #define AQUA_PRECISION_FAST 1
 aqua_status aqua_set_precision(aqua_ctx* ctx, int mode);
 
-/* Launch shape of the sweep: `sweep_variant` selects threads per block and
- * queued neighbours per thread (0: 128 x 128, 1: 64 x 128, 2: 128 x 64,
- * 3: 256 x 64), `blocks_per_sm` the persistent grid (blocks per SM).  Any
- * choice gives the same results; aquagpusph_gb300.autotune picks the
+/* Launch shape of the sweep: `sweep_variant` selects threads per block,
+ * queued neighbours per thread and the queue entry (0: 128 x 128 16-bit,
+ * 1: 64 x 128 16-bit, 2: 64 x 64 32-bit, 3: 128 x 64 32-bit),
+ * `blocks_per_sm` the persistent grid (blocks per SM, <= 32).
+ * Any choice gives the same results; aquagpusph_gb300.autotune picks the
  * fastest for a case by timing them. */
 aqua_status aqua_set_tuning(aqua_ctx* ctx, uint32_t sweep_variant,
                             uint32_t blocks_per_sm);
