@@ -170,36 +170,66 @@ k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
 // n_cells of every case from its bounding box (LinkList::nCells, float
 // division), the first global cell key of each case, and the capacity check
 template<int D>
-__global__ void
+__global__ void __launch_bounds__(1024)
 k_ncells(Consts c, CaseScalars* cs, uint32_t n_cases, DevScalars* sc,
          uint32_t ncap)
 {
-    if (threadIdx.x != 0 || sc->err)
-        return;
-    unsigned long long base = 0;
-    for (uint32_t k = 0; k < n_cases; k++) {
-        unsigned long long nn[3] = { 1, 1, 1 };
-        bool ok = true;
+    // one block; thread t handles cases [t * per, t * per + per), per <= 4
+    __shared__ unsigned long long part[1024];
+    __shared__ int bad;
+    if (sc->err)
+        return;  // the same value for every thread of the block
+    if (threadIdx.x == 0)
+        bad = 0;
+    __syncthreads();
+    const uint32_t per = (n_cases + blockDim.x - 1) / blockDim.x;
+    const uint32_t k0 = threadIdx.x * per;
+    unsigned long long nw[4] = { 0, 0, 0, 0 };
+    unsigned long long nn[4][3];
+    unsigned long long sum = 0;
+    for (uint32_t j = 0; j < per && j < 4; j++) {
+        const uint32_t k = k0 + j;
+        if (k >= n_cases)
+            break;
+        nn[j][0] = nn[j][1] = nn[j][2] = 1;
         for (int d = 0; d < D; d++) {
             const float span = (cs[k].r_max[d] - cs[k].r_min[d]) / c.cell_length;
             if (!(span >= 0.f) || span > 4.0e9f)
-                ok = false;
+                bad = 1;
             else
-                nn[d] = (unsigned long long)span + 6ull;
+                nn[j][d] = (unsigned long long)span + 6ull;
         }
-        const unsigned long long nw = nn[0] * nn[1] * nn[2];
-        if (!ok || base + nw > ncap) {
-            atomicOr(&sc->err, kErrCapacity);
-            return;
-        }
-        cs[k].n_cells[0] = (uint32_t)nn[0];
-        cs[k].n_cells[1] = (uint32_t)nn[1];
-        cs[k].n_cells[2] = (uint32_t)nn[2];
-        cs[k].n_cells[3] = (uint32_t)nw;
-        cs[k].cell_base = (uint32_t)base;
-        base += nw;
+        nw[j] = nn[j][0] * nn[j][1] * nn[j][2];
+        sum += nw[j];
     }
-    sc->total_cells = (uint32_t)base;
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+        const unsigned long long v = threadIdx.x >= off ? part[threadIdx.x - off] : 0ull;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    const unsigned long long total = part[blockDim.x - 1];
+    if (bad || total > ncap) {
+        if (threadIdx.x == 0)
+            atomicOr(&sc->err, kErrCapacity);
+        return;
+    }
+    unsigned long long base = part[threadIdx.x] - sum;
+    for (uint32_t j = 0; j < per && j < 4; j++) {
+        const uint32_t k = k0 + j;
+        if (k >= n_cases)
+            break;
+        cs[k].n_cells[0] = (uint32_t)nn[j][0];
+        cs[k].n_cells[1] = (uint32_t)nn[j][1];
+        cs[k].n_cells[2] = (uint32_t)nn[j][2];
+        cs[k].n_cells[3] = (uint32_t)nw[j];
+        cs[k].cell_base = (uint32_t)base;
+        base += nw[j];
+    }
+    if (threadIdx.x == 0)
+        sc->total_cells = (uint32_t)total;
 }
 
 template<int D>
@@ -498,7 +528,7 @@ cudaError_t
 launch_ncells(const Consts& c, CaseScalars* cs, uint32_t n_cases, DevScalars* sc,
               uint32_t ncap, cudaStream_t s)
 {
-    k_ncells<D><<<1, 32, 0, s>>>(c, cs, n_cases, sc, ncap);
+    k_ncells<D><<<1, 1024, 0, s>>>(c, cs, n_cases, sc, ncap);
     return cudaGetLastError();
 }
 
