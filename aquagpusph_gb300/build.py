@@ -22,7 +22,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libaqua_gb300.so")
 SOURCES = ("linklist.cu", "step.cu", "step_fast.cu", "api.cu", "noalloc.cu",
-           "output.cu", "fastascii.cpp", "gnn.cu")
+           "output.cu", "fastascii.cpp", "gnn.cu", "gnn_tc.cu")
 # per-file arithmetic: the fast step kernels trade the reference's exact
 # rounding for FMA contraction and approximate division / square root
 FAST_MATH = {"step_fast.cu"}

@@ -1,0 +1,242 @@
+// Dense-layer forward of the learned proposal on the 5th-generation tensor
+// cores: Y = act(X W^T + b) with tcgen05.mma (kind::f16, BF16 x BF16 ->
+// FP32) accumulating in tensor memory.  No counterpart in the reference.
+//
+// One CTA of 128 threads works on tiles of 128 rows:
+//   - W (N x K) is staged once in shared memory, X tiles (128 x K) per tile,
+//     both in the K-major layout without swizzle: 8-row x 16-byte core
+//     matrices, consecutive along K (leading byte offset 128 B), row groups
+//     K/8 core matrices apart (stride byte offset);
+//   - thread 0 issues K/16 MMAs of 128 x N x 16 into an N-column TMEM
+//     accumulator and commits them to an mbarrier;
+//   - every warp reads its 32 TMEM lanes (rows) back with tcgen05.ld, adds
+//     the bias, applies the activation and stores Z (f32) and / or Y (bf16).
+// Every wait on the mbarrier is bounded: on time-out the kernel records
+// an error, skips the tile's stores, frees its TMEM and returns.
+#include <cuda_bf16.h>
+#include <cstdint>
+
+#include "aqua_learned.h"
+
+namespace {
+
+constexpr int kTcThreads = 128;
+constexpr int kTcRows = 128;
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t
+smem_addr(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle
+__device__ __forceinline__ uint64_t
+make_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+    d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version of tcgen05
+    return d;                // base offset 0, swizzle none
+}
+
+// instruction descriptor of kind::f16: D f32, A and B bf16, both K-major,
+// M = 128, N = n
+__host__ __device__ constexpr uint32_t
+make_idesc(uint32_t n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) |
+           ((uint32_t)(kTcRows >> 4) << 24);
+}
+
+__device__ __forceinline__ float
+silu_f(float z)
+{
+    return z / (1.f + expf(-z));
+}
+
+__device__ __forceinline__ uint32_t
+pack2(float lo, float hi)
+{
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+}
+
+// copy a rows x K bf16 block (row-major, ld elements) into the core-matrix
+// layout: element (r, k) at ((r / 8) * (K / 8) + k / 8) * 128 + (r % 8) * 16
+// + (k % 8) * 2 bytes; rows past `valid` are zero
+__device__ __forceinline__ void
+stage(uint8_t* dst, const uint16_t* src, uint32_t ld, uint32_t rows,
+      uint32_t valid, uint32_t K)
+{
+    const uint32_t kg = K / 8;
+    for (uint32_t e = threadIdx.x; e < rows * kg; e += kTcThreads) {
+        const uint32_t r = e / kg, g = e % kg;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (r < valid)
+            v = *reinterpret_cast<const uint4*>(src + (size_t)r * ld + g * 8);
+        *reinterpret_cast<uint4*>(dst + ((r / 8) * kg + g) * 128 + (r % 8) * 16) = v;
+    }
+}
+
+template<int N>
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_linear_fwd_tc(uint32_t M, uint32_t K, const uint16_t* __restrict__ X,
+                uint32_t ldx, const uint16_t* __restrict__ W,
+                const float* __restrict__ bias, float* Z, uint32_t ldz,
+                uint16_t* Y, uint32_t ldy, int act, int* err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sB = smem;                                // N x K
+    uint8_t* sA = smem + ((N * K * 2 + 1023) / 1024) * 1024;  // 128 x K
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    stage(sB, W, K, N, N, K);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n"
+                     :: "r"(smem_addr(&mbar)));
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 "
+                     "[%0], %1;\n" :: "r"(smem_addr(&tmem_base)), "r"((uint32_t)N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = make_idesc(N);
+    const uint32_t kg = K / 8;
+    const uint32_t sbo = kg * 128;  // next 8-row group
+    uint32_t phase = 0;
+    bool failed = false;
+    const uint32_t tiles = (M + kTcRows - 1) / kTcRows;
+    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const uint32_t m0 = tile * kTcRows;
+        const uint32_t valid = min((uint32_t)kTcRows, M - m0);
+        stage(sA, X + (size_t)m0 * ldx, ldx, kTcRows, valid, K);
+        // generic-proxy stores -> visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;\n");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            for (uint32_t ks = 0; ks < K / 16; ks++) {
+                const uint64_t ad = make_desc(smem_addr(sA) + ks * 256, 128, sbo);
+                const uint64_t bd = make_desc(smem_addr(sB) + ks * 256, 128, sbo);
+                const uint32_t acc = ks > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                    :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one."
+                         "shared::cluster.b64 [%0];\n" :: "r"(smem_addr(&mbar)));
+        }
+        // bounded wait for the MMAs of this tile
+        uint32_t done = 0;
+        for (uint32_t it = 0; it < kWaitLimit && !done; it++) {
+            asm volatile("{\n.reg .pred p;\n"
+                         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                         "selp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(done) : "r"(smem_addr(&mbar)), "r"(phase));
+        }
+        if (!__all_sync(0xffffffffu, done)) {
+            failed = true;
+            if (lane == 0)
+                atomicExch(err, 1);
+        }
+        failed = __syncthreads_or(failed);
+        if (failed)
+            break;
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        // epilogue: warp w owns rows 32w .. 32w + 31 (TMEM lanes)
+        const uint32_t row = m0 + warp * 32 + lane;
+        const uint32_t taddr = tmem + ((warp * 32u) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+                  "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+                  "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                  "=r"(v[14]), "=r"(v[15])
+                : "r"(taddr + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+            if (row < M) {
+                float z[16];
+                for (int j = 0; j < 16; j++)
+                    z[j] = __uint_as_float(v[j]) + (bias ? bias[c0 + j] : 0.f);
+                if (Z)
+                    for (int j = 0; j < 16; j += 4)
+                        *reinterpret_cast<float4*>(Z + (size_t)row * ldz + c0 + j) =
+                            make_float4(z[j], z[j + 1], z[j + 2], z[j + 3]);
+                if (Y) {
+                    uint32_t p[8];
+                    for (int j = 0; j < 8; j++) {
+                        const float a0 = act == AQUA_ACT_SILU ? silu_f(z[2 * j]) : z[2 * j];
+                        const float a1 = act == AQUA_ACT_SILU ? silu_f(z[2 * j + 1]) : z[2 * j + 1];
+                        p[j] = pack2(a0, a1);
+                    }
+                    uint4* dst = reinterpret_cast<uint4*>(Y + (size_t)row * ldy + c0);
+                    dst[0] = make_uint4(p[0], p[1], p[2], p[3]);
+                    dst[1] = make_uint4(p[4], p[5], p[6], p[7]);
+                }
+            }
+        }
+        // the next tile's MMAs overwrite the accumulator and sA
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncthreads();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n"
+                     :: "r"(tmem), "r"((uint32_t)N));
+    }
+}
+
+}  // namespace
+
+extern "C" aqua_status
+aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N, const uint16_t* X,
+                       uint32_t ldx, const uint16_t* W, const float* b,
+                       float* Z, uint32_t ldz, uint16_t* Y, uint32_t ldy,
+                       int32_t act, int32_t* err, void* stream)
+{
+    if (!X || !W || !err || (!Z && !Y) || K == 0 || K % 16 || K > 160 ||
+        N != 64 || ldx < K || ldx % 8 || (Z && (ldz < N || ldz % 4)) ||
+        (Y && (ldy < N || ldy % 8)) ||
+        (reinterpret_cast<uintptr_t>(X) & 15) || (reinterpret_cast<uintptr_t>(W) & 15) ||
+        (Z && (reinterpret_cast<uintptr_t>(Z) & 15)) ||
+        (Y && (reinterpret_cast<uintptr_t>(Y) & 15)))
+        return AQUA_ERR_INVALID;
+    if (M == 0)
+        return AQUA_OK;
+    const size_t bytes = ((size_t)N * K * 2 + 1023) / 1024 * 1024 +
+                         (size_t)kTcRows * K * 2;
+    static bool configured = false;
+    if (!configured) {
+        if (cudaFuncSetAttribute(k_linear_fwd_tc<64>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 64 * 1024) != cudaSuccess)
+            return AQUA_ERR_CUDA;
+        configured = true;
+    }
+    int sms = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+            cudaSuccess)
+        return AQUA_ERR_CUDA;
+    const uint32_t tiles = (M + kTcRows - 1) / kTcRows;
+    const uint32_t grid = tiles < (uint32_t)sms * 4u ? tiles : (uint32_t)sms * 4u;
+    k_linear_fwd_tc<64><<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
+        M, K, X, ldx, W, b, Z, ldz, Y, ldy, act, err);
+    return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
+}

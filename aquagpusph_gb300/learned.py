@@ -77,7 +77,9 @@ SIGNATURES = {
                                    _vp, _vp, _vp],
         "aqua_gnn_linear_fwd": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32, _vp,
                                 _u32, _i32, _vp],
-        "aqua_gnn_linear_dgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _u32, _i32,
+        "aqua_gnn_linear_fwd_tc": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32,
+                               _vp, _u32, _i32, _vp, _vp],
+    "aqua_gnn_linear_dgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _u32, _i32,
                                   _vp, _u32, _vp],
         "aqua_gnn_linear_wgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _u32, _vp, _vp, _vp],
         "aqua_gnn_segment_sum": [_u32, _vp, _vp, _u32, _f32, _vp, _u32, _u32, _vp],

@@ -114,6 +114,15 @@ aqua_status aqua_gnn_linear_fwd(uint32_t M, uint32_t K, uint32_t N,
                                 const uint16_t* W, const float* b, float* Z,
                                 uint32_t ldz, uint16_t* Y, uint32_t ldy,
                                 int32_t act, void* stream);
+/* The same forward on the 5th-generation tensor cores (tcgen05.mma with a
+ * tensor-memory accumulator, 128-row tiles), for N = 64: all pointers
+ * 16-byte aligned, ldz % 4 == 0.  A time-out of its bounded waits sets
+ * *err (device int, set to 0 by the caller) instead of hanging. */
+aqua_status aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N,
+                                   const uint16_t* X, uint32_t ldx,
+                                   const uint16_t* W, const float* b, float* Z,
+                                   uint32_t ldz, uint16_t* Y, uint32_t ldy,
+                                   int32_t act, int32_t* err, void* stream);
 /* dX = dY W (M x K, bf16 at ldx) where dY: M x N bf16 (ldy), Wt: K x N.
  * With Zprev (M x K f32, ldzp) and act_prev = AQUA_ACT_SILU the result is
  * multiplied by silu'(Zprev) (the gradient of the previous layer's
