@@ -38,6 +38,9 @@ LAYERS = [
     ("n2_0", 64, 144, 1), ("n2_1", 64, 64, 1), ("n2_2", 16, 64, 0),
 ]
 AGG_SCALE = 1.0 / 32.0
+# 64-wide layers run on tcgen05 (tensor memory) when True, on mma.sync
+# otherwise (the 16-wide output layer always uses mma.sync)
+USE_TCGEN05 = True
 
 _vp = C.c_void_p
 
@@ -335,10 +338,14 @@ class Inputs:
 class Network:
     """Forward (and, with ``train``, backward) of the model on one graph."""
 
-    def __init__(self, model: Model, graph: Graph, inputs: Inputs, stream=None):
+    def __init__(self, model: Model, graph: Graph, inputs: Inputs, stream=None,
+                 tcgen05=None):
+        torch = _torch()
         self.model, self.g, self.x = model, graph, inputs
         self.s = _vp(stream or 0)
         self.stream = stream
+        self.tc = USE_TCGEN05 if tcgen05 is None else bool(tcgen05)
+        self.err = torch.zeros(1, dtype=torch.int32, device=graph.rs.device)
 
     def _buf(self, shape, dtype):
         torch = _torch()
@@ -346,6 +353,11 @@ class Network:
 
     def _lin(self, name, X, ldx, M, Z=None, ldz=0, Y=None, ldy=0):
         o, ob, n, k, act = self.model.offs[name]
+        if self.tc and n == 64:
+            _chk("aqua_gnn_linear_fwd_tc", lib().aqua_gnn_linear_fwd_tc(
+                M, k, n, X, ldx, self.model.W(name), self.model.b(name),
+                Z, ldz, Y, ldy, act, _p(self.err), self.s))
+            return
         _chk("aqua_gnn_linear_fwd", lib().aqua_gnn_linear_fwd(
             M, k, n, X, ldx, self.model.W(name), self.model.b(name),
             Z, ldz, Y, ldy, act, self.s))
@@ -429,6 +441,9 @@ class Network:
         c["n2"] = (A2, Z2)
         self.cache = c
         self.out = out
+        if self.tc and int(self.err.item()):
+            raise _lib.AquaError("aqua_gnn_linear_fwd_tc (wait timed out)",
+                                 _lib.AQUA_ERR_CUDA)
         return out
 
     def _mlp_bwd(self, prefix, X, ldx, A, Z, dY, M, want_dx, dx_ld=None):

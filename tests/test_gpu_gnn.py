@@ -118,7 +118,8 @@ def network_inputs(torch, b, seed=0):
     return sv, g, x, host
 
 
-def test_network_forward_backward_match_oracle(torch):
+@pytest.mark.parametrize("tcgen05", [False, True])
+def test_network_forward_backward_match_oracle(torch, tcgen05):
     from aquagpusph_gb300 import learned as Lm
     b = small_batch(2)
     c = b.case
@@ -130,7 +131,7 @@ def test_network_forward_backward_match_oracle(torch):
     model = Lm.Model(2, params)
     sc = (float(c.params.h), 0.05, 0.5, 0.5, 5.0, 998.0)
     model.scales.copy_(torch.tensor(sc))
-    net = Lm.Network(model, g, x)
+    net = Lm.Network(model, g, x, tcgen05=tcgen05)
     out = net.forward(train=True)
     n = g.n_nodes
     target = rng.normal(0, 1, (n, 3)).astype(np.float32)
