@@ -23,6 +23,7 @@ AQUA_ERR_NO_MEMORY = -5
 AQUA_ERR_NONFINITE = -6
 AQUA_ERR_IO = -7
 AQUA_ERR_FORMAT = -8
+AQUA_ERR_TIMEOUT = -9
 
 AQUA_PRECISION_EXACT = 0
 AQUA_PRECISION_FAST = 1
@@ -48,6 +49,7 @@ STATUS_NAMES = {
     AQUA_ERR_NONFINITE: "AQUA_ERR_NONFINITE",
     AQUA_ERR_IO: "AQUA_ERR_IO",
     AQUA_ERR_FORMAT: "AQUA_ERR_FORMAT",
+    AQUA_ERR_TIMEOUT: "AQUA_ERR_TIMEOUT",
 }
 
 _F = C.POINTER(C.c_float)

@@ -18,8 +18,10 @@ import time
 from . import _lib
 
 # (variant, threads per block, queued neighbours per thread); the variant
-# numbers are those of aqua_set_tuning
-VARIANTS = ((0, 128, 128), (1, 64, 128), (2, 64, 64), (3, 128, 64))
+# numbers are those of aqua_set_tuning (3 and 4 stage the candidates with
+# bulk copies)
+VARIANTS = ((0, 128, 128), (1, 64, 128), (2, 64, 64), (3, 64, 128),
+            (4, 64, 64))
 # resident warps per SM tried for each variant (blocks = warps * 32 / threads)
 WARPS_PER_SM = (8, 10, 12, 16, 20, 24)
 MAX_BLOCKS_PER_SM = 32

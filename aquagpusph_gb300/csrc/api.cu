@@ -337,6 +337,8 @@ status_of(uint32_t err)
         return AQUA_ERR_NONFINITE;
     if (err & kErrDt)
         return AQUA_ERR_DT;
+    if (err & kErrTimeout)
+        return AQUA_ERR_TIMEOUT;
     return AQUA_OK;
 }
 

@@ -24,6 +24,7 @@ enum : uint32_t
     kErrCapacity = 1u << 0,
     kErrDt = 1u << 1,
     kErrNonFinite = 1u << 2,
+    kErrTimeout = 1u << 3,   // a bounded wait in a kernel ran out
 };
 
 // Case constants as the kernels see them (__constant__ copy per launch set)

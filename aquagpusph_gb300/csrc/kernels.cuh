@@ -9,13 +9,14 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
 // sweep variants: threads per block x queued neighbours per thread (the
-// staging depth) x queue entry: 0 = (128, 128, 16-bit), 1 = (64, 128,
-// 16-bit), 2 = (64, 64, 32-bit), 3 = (128, 64, 32-bit)
-constexpr int kSweepVariants = 4;
+// staging depth) x queue entry x candidate staging: 0 = (128, 128, 16-bit,
+// loads), 1 = (64, 128, 16-bit, loads), 2 = (64, 64, 32-bit, loads),
+// 3 = (64, 128, 16-bit, bulk copies), 4 = (64, 64, 32-bit, bulk copies)
+constexpr int kSweepVariants = 5;
 inline int
 sweep_variant_threads(int v)
 {
-    return (v == 1 || v == 2) ? 64 : 128;
+    return v == 0 ? 128 : 64;
 }
 
 // The reference's vec type: float4 in 3-D, float2 in 2-D

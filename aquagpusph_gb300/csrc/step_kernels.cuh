@@ -41,6 +41,8 @@
 
 namespace {
 
+constexpr uint32_t kBulkWaitLimit = 1u << 20;  // bounded mbarrier polls
+
 // Wendland C2 (Wendland{2D,3D}.hcl:44-66); the constants are float
 // products folded at compile time, as the OpenCL compiler folds them
 template<int D>
@@ -283,10 +285,11 @@ k_gather(Consts c, StepArgs a)
 // neighbour cells of the warp's cell.  The scan checks the queues every 32
 // candidates, where they have room for at least 32 more, so a queue never
 // overflows.
-template<int D, int NT, int NQ, typename QE>
+template<int D, int NT, int NQ, typename QE, bool BULK>
 __device__ __forceinline__ float
 sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
-               QE* queue, uint32_t* cstart, float4* grp)
+               QE* queue, uint32_t* cstart, float4* grp2, uint64_t* mbar,
+               uint32_t& phases)
 {
     constexpr int VS = Vec<D>::VS;
     constexpr int NC = (D == 3) ? 27 : 9;
@@ -420,82 +423,152 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
             cstart[lane] = a.b.cells[neighbour_cell<D>(key_i, lane, nx, nxy)].x;
         __syncwarp();
     }
-    for (int k = 0; k < NC; k++) {
-        const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
-        const uint2 se = a.b.cells[cn];
+    // The candidates are visited in groups of up to 32 (cell by cell, in the
+    // reference order).  With BULK the bulk-copy engine copies each group's
+    // packed positions into a shared-memory buffer one group ahead (two
+    // buffers per warp, completion tracked by an mbarrier each), so the copy
+    // of the next group overlaps the work on the current one; without it
+    // the lanes load the group themselves (one coalesced load).
+    auto advance = [&](int& kk, uint2& se, uint32_t& g) -> bool {
+        g += 32u;
+        while (g >= se.y - se.x) {
+            if (++kk >= NC)
+                return false;
+            se = a.b.cells[neighbour_cell<D>(key_i, kk, nx, nxy)];
+            g = 0;
+            if (sizeof(QE) == 2 && se.y - se.x > 2048u) {
+                // the 11-bit offsets cannot address such a cell
+                if (lane == 0)
+                    atomicOr(&a.sc->err, kErrCapacity);
+                se.y = se.x;
+            }
+        }
+        return true;
+    };
+    auto issue = [&](int b, const uint2 se, uint32_t g) {
+        if (BULK && lane == 0) {
+            const uint32_t bytes = min(32u, se.y - se.x - g) * 16u;
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[b]);
+            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(grp2 + 32 * b);
+            const uint64_t src = (uint64_t)__cvta_generic_to_global(a.b.posq + se.x + g);
+            // earlier generic reads of the buffer before the async write
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n"
+                         :: "r"(mb), "r"(bytes) : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                         "[%0], [%1], %2, [%3];\n"
+                         :: "r"(dst), "l"(src), "r"(bytes), "r"(mb) : "memory");
+        }
+    };
+    auto wait = [&](int b) -> bool {
+        const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[b]);
+        const uint32_t par = (phases >> b) & 1u;
+        uint32_t done = 0;
+        for (uint32_t it = 0; it < kBulkWaitLimit && !done; it++)
+            asm volatile("{\n.reg .pred p;\n"
+                         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                         "selp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(done) : "r"(mb), "r"(par) : "memory");
+        phases ^= 1u << b;
+        return __all_sync(0xffffffffu, done != 0);
+    };
+
+    int k = -1;
+    uint2 se = make_uint2(0u, 0u);
+    uint32_t g = 0xFFFFFFE0u;  // advance() wraps it to the first group
+    bool have = advance(k, se, g);
+    int buf = 0;
+    if (BULK && have)
+        issue(0, se, g);
+    while (have) {
+        int kn = k;
+        uint2 sen = se;
+        uint32_t gn = g;
+        const bool hn = advance(kn, sen, gn);
+        if (BULK && hn)
+            issue(buf ^ 1, sen, gn);
+        // warp-uniform checkpoint: make room for the next 32 candidates,
+        // first draining the entries every lane has (full warps)
+        if (__any_sync(0xffffffffu, qt - qh > NQ - 32)) {
+            const uint32_t fill = qt - qh;
+            const uint32_t common = __reduce_min_sync(
+                0xffffffffu, want_shep ? fill : 0xffffffffu);
+            drain(qh + min(common, fill));
+            if (__any_sync(0xffffffffu, qt - qh > NQ - 32))
+                drain(qt);
+        }
         const uint32_t count = se.y - se.x;
-        if (sizeof(QE) == 2 && count > 2048u) {
-            // the 11-bit offsets cannot address such a cell
-            if (lane == 0)
-                atomicOr(&a.sc->err, kErrCapacity);
-            continue;
-        }
-        for (uint32_t g = 0; g < count; g += 32) {
-            // warp-uniform checkpoint: make room for the next 32 candidates,
-            // first draining the entries every lane has (full warps)
-            if (__any_sync(0xffffffffu, qt - qh > NQ - 32)) {
-                const uint32_t fill = qt - qh;
-                const uint32_t common = __reduce_min_sync(
-                    0xffffffffu, want_shep ? fill : 0xffffffffu);
-                drain(qh + min(common, fill));
-                if (__any_sync(0xffffffffu, qt - qh > NQ - 32))
-                    drain(qt);
+        const uint32_t gend = min(g + 32u, count);
+        float4* grp = grp2 + 32 * buf;
+        if constexpr (BULK) {
+            if (!wait(buf)) {
+                if (lane == 0)
+                    atomicOr(&a.sc->err, kErrTimeout);
+                if (hn)
+                    wait(buf ^ 1);  // the copy in flight, again bounded
+                break;
             }
-            const uint32_t gend = min(g + 32u, count);
-            // lane-parallel pre-filter of the 32 candidates of this group:
-            // drop those farther than the support from the box of the
-            // chunk's particles (no lane can take them); the survivors are
-            // then tested per lane in their visiting order
-            bool cand = false;
-            if (g + lane < gend) {
-                const float4 pc = a.b.posq[se.x + g + lane];
-                grp[lane] = pc;
-                const int jm = __float_as_int(pc.w);
-                const float bx = fmaxf(fmaxf(blo[0] - pc.x, pc.x - bhi[0]), 0.f);
-                const float by = fmaxf(fmaxf(blo[1] - pc.y, pc.y - bhi[1]), 0.f);
-                float bb = bx * bx + by * by;
-                if (D == 3) {
-                    const float bz = fmaxf(fmaxf(blo[2] - pc.z, pc.z - bhi[2]), 0.f);
-                    bb = bb + bz * bz;
-                }
-                cand = (jm == 1 || jm == -3) && bb < q2_box;
-            }
-            uint32_t bal = __ballot_sync(0xffffffffu, cand);
+        } else {
+            if (g + lane < gend)
+                grp[lane] = a.b.posq[se.x + g + lane];
             __syncwarp();
-            auto consider = [&](const float4 pj, uint32_t off) {
-                const int jm = __float_as_int(pj.w);
-                const float d0 = pj.x - ri[0], d1 = pj.y - ri[1];
-                float rr = d0 * d0 + d1 * d1;
-                if (D == 3) {
-                    const float d2 = pj.z - ri[2];
-                    rr = rr + d2 * d2;
-                }
-                const bool take = want_shep && (jm == 1 || (fluid && jm == -3)) &&
-                                  rr < c.q2_reject;
-                if (take) {
-                    if constexpr (sizeof(QE) == 2)
-                        queue[(qt & (NQ - 1)) * NT] = (QE)(((uint32_t)k << 11) | off);
-                    else
-                        queue[(qt & (NQ - 1)) * NT] = se.x + off;
-                    qt++;
-                }
-            };
-            while (bal) {
-                // two survivors per iteration, in visiting order
-                const uint32_t b0 = __ffs(bal) - 1;
-                bal &= bal - 1;
-                const bool two = bal != 0;
-                const uint32_t b1 = two ? (uint32_t)(__ffs(bal) - 1) : b0;
-                if (two)
-                    bal &= bal - 1;
-                const float4 p0 = grp[b0];
-                const float4 p1 = grp[b1];
-                consider(p0, g + b0);
-                if (two)
-                    consider(p1, g + b1);
-            }
-            __syncwarp();  // grp is rewritten by the next group
         }
+        // lane-parallel pre-filter of the candidates of this group: drop
+        // those farther than the support from the box of the chunk's
+        // particles (no lane can take them); the survivors are then tested
+        // per lane in their visiting order
+        bool cand = false;
+        if (g + lane < gend) {
+            const float4 pc = grp[lane];
+            const int jm = __float_as_int(pc.w);
+            const float bx = fmaxf(fmaxf(blo[0] - pc.x, pc.x - bhi[0]), 0.f);
+            const float by = fmaxf(fmaxf(blo[1] - pc.y, pc.y - bhi[1]), 0.f);
+            float bb = bx * bx + by * by;
+            if (D == 3) {
+                const float bz = fmaxf(fmaxf(blo[2] - pc.z, pc.z - bhi[2]), 0.f);
+                bb = bb + bz * bz;
+            }
+            cand = (jm == 1 || jm == -3) && bb < q2_box;
+        }
+        uint32_t bal = __ballot_sync(0xffffffffu, cand);
+        auto consider = [&](const float4 pj, uint32_t off) {
+            const int jm = __float_as_int(pj.w);
+            const float d0 = pj.x - ri[0], d1 = pj.y - ri[1];
+            float rr = d0 * d0 + d1 * d1;
+            if (D == 3) {
+                const float d2 = pj.z - ri[2];
+                rr = rr + d2 * d2;
+            }
+            const bool take = want_shep && (jm == 1 || (fluid && jm == -3)) &&
+                              rr < c.q2_reject;
+            if (take) {
+                if constexpr (sizeof(QE) == 2)
+                    queue[(qt & (NQ - 1)) * NT] = (QE)(((uint32_t)k << 11) | off);
+                else
+                    queue[(qt & (NQ - 1)) * NT] = se.x + off;
+                qt++;
+            }
+        };
+        while (bal) {
+            // two survivors per iteration, in visiting order
+            const uint32_t b0 = __ffs(bal) - 1;
+            bal &= bal - 1;
+            const bool two = bal != 0;
+            const uint32_t b1 = two ? (uint32_t)(__ffs(bal) - 1) : b0;
+            if (two)
+                bal &= bal - 1;
+            const float4 p0 = grp[b0];
+            const float4 p1 = grp[b1];
+            consider(p0, g + b0);
+            if (two)
+                consider(p1, g + b1);
+        }
+        __syncwarp();  // the buffer is rewritten by the group after next
+        k = kn;
+        se = sen;
+        g = gn;
+        have = hn;
+        buf ^= 1;
     }
     drain(qt);
     if (!valid)
@@ -676,15 +749,23 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
 
 // Persistent sweep: warps fetch cell-aligned chunks of <= 32 particles
 // NT threads per block, NQ queued neighbours per thread (power of 2, >= 64)
-// of type QE
-template<int D, int NT, int NQ, typename QE>
+// of type QE, candidate groups copied by the bulk-copy engine when BULK
+template<int D, int NT, int NQ, typename QE, bool BULK>
 __global__ void __launch_bounds__(NT, 640 / NT)
 k_sweep(Consts c, StepArgs a)
 {
     __shared__ QE s_queue[NQ * NT];
     __shared__ uint32_t s_cstart[NT / 32][32];
-    __shared__ float4 s_grp[NT / 32][32];
+    __shared__ __align__(16) float4 s_grp[NT / 32][2 * 32];
+    __shared__ __align__(8) uint64_t s_mbar[NT / 32][2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < (NT / 32) * 2) {
+        const uint32_t mb = (uint32_t)__cvta_generic_to_shared(
+            &s_mbar[threadIdx.x >> 1][threadIdx.x & 1]);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(mb));
+    }
+    __syncthreads();
+    uint32_t phases = 0;  // parity of the next completion of each buffer
     // running minimum of dt_var of the warp's current case, flushed to the
     // case's dt_next when the case changes and at the end
     float run_min = INFINITY;
@@ -708,9 +789,9 @@ k_sweep(Consts c, StepArgs a)
                 break;
             const uint2 cw = a.b.chunks[ch];
             const bool valid = (uint32_t)lane < cw.y;
-            float v = sweep_particle<D, NT, NQ, QE>(
+            float v = sweep_particle<D, NT, NQ, QE, BULK>(
                 c, a, valid ? cw.x + lane : cw.x, valid, s_queue + threadIdx.x,
-                s_cstart[warp], s_grp[warp]);
+                s_cstart[warp], s_grp[warp], s_mbar[warp], phases);
             __syncwarp();  // s_cstart and s_grp are rewritten for the next chunk
             for (int o = 16; o > 0; o >>= 1)
                 v = cl_min(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -737,7 +818,8 @@ launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s)
 }
 
 // sweep variants the tuner chooses from: (threads per block, queue depth,
-// queue entry type); the static shared memory of a block stays <= 34 KB
+// queue entry type, bulk-copy staging); a block's static shared memory
+// stays <= 37 KB
 template<int D>
 cudaError_t
 launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
@@ -747,16 +829,19 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
         return cudaSuccess;
     switch (variant) {
     case 1:
-        k_sweep<D, 64, 128, uint16_t><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 128, uint16_t, false><<<grid, 64, 0, s>>>(c, a);
         break;
     case 2:
-        k_sweep<D, 64, 64, uint32_t><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 64, uint32_t, false><<<grid, 64, 0, s>>>(c, a);
         break;
     case 3:
-        k_sweep<D, 128, 64, uint32_t><<<grid, 128, 0, s>>>(c, a);
+        k_sweep<D, 64, 128, uint16_t, true><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 4:
+        k_sweep<D, 64, 64, uint32_t, true><<<grid, 64, 0, s>>>(c, a);
         break;
     default:
-        k_sweep<D, 128, 128, uint16_t><<<grid, 128, 0, s>>>(c, a);
+        k_sweep<D, 128, 128, uint16_t, false><<<grid, 128, 0, s>>>(c, a);
         break;
     }
     return cudaGetLastError();

@@ -48,7 +48,8 @@ typedef enum
     AQUA_ERR_NO_MEMORY = -5,   /* device allocation failed */
     AQUA_ERR_NONFINITE = -6,   /* non-finite position reached the link-list */
     AQUA_ERR_IO = -7,          /* a file could not be opened or read */
-    AQUA_ERR_FORMAT = -8       /* a particles file line is malformed */
+    AQUA_ERR_FORMAT = -8,      /* a particles file line is malformed */
+    AQUA_ERR_TIMEOUT = -9      /* a bounded wait inside a kernel ran out */
 } aqua_status;
 
 /* Scalar Variables and Definitions of one case.  The Definitions are the
@@ -190,9 +191,11 @@ aqua_status aqua_set_extras(aqua_ctx* ctx, int on);
 aqua_status aqua_set_precision(aqua_ctx* ctx, int mode);
 
 /* Launch shape of the sweep: `sweep_variant` selects threads per block,
- * queued neighbours per thread and the queue entry (0: 128 x 128 16-bit,
- * 1: 64 x 128 16-bit, 2: 64 x 64 32-bit, 3: 128 x 64 32-bit),
- * `blocks_per_sm` the persistent grid (blocks per SM, <= 32).
+ * queued neighbours per thread, the queue entry and how candidate groups
+ * reach shared memory (0: 128 x 128 16-bit loads, 1: 64 x 128 16-bit loads,
+ * 2: 64 x 64 32-bit loads, 3: 64 x 128 16-bit bulk copies, 4: 64 x 64
+ * 32-bit bulk copies), `blocks_per_sm` the persistent grid (blocks per SM,
+ * <= 32).
  * Any choice gives the same results; aquagpusph_gb300.autotune picks the
  * fastest for a case by timing them. */
 aqua_status aqua_set_tuning(aqua_ctx* ctx, uint32_t sweep_variant,
@@ -236,8 +239,9 @@ aqua_status aqua_step(aqua_ctx* ctx, uint32_t nsteps, int use_graph,
                       void* stream);
 
 /* Synchronises `stream` and returns the first error a kernel recorded since
- * the last call (AQUA_ERR_CAPACITY, AQUA_ERR_DT, AQUA_ERR_NONFINITE), then
- * clears it.  The step skips its remaining work once an error is set. */
+ * the last call (AQUA_ERR_CAPACITY, AQUA_ERR_DT, AQUA_ERR_NONFINITE,
+ * AQUA_ERR_TIMEOUT), then clears it.  The step skips its remaining work
+ * once an error is set. */
 aqua_status aqua_check(aqua_ctx* ctx, void* stream);
 
 /* The link-list tool on caller-owned device buffers (LinkList.cpp:326-494):

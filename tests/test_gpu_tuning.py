@@ -42,7 +42,7 @@ def run(c, variant, blocks, steps=3, fast=False):
     return g
 
 
-SHAPES = [(0, 2), (0, 5), (1, 10), (2, 4), (3, 2), (3, 8)]
+SHAPES = [(0, 2), (0, 5), (1, 10), (2, 4), (3, 8), (4, 12)]
 
 
 @pytest.mark.parametrize("fast", [False, True])
