@@ -235,7 +235,8 @@ aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N, const uint16_t* X,
             cudaSuccess)
         return AQUA_ERR_CUDA;
     const uint32_t tiles = (M + kTcRows - 1) / kTcRows;
-    const uint32_t grid = tiles < (uint32_t)sms * 4u ? tiles : (uint32_t)sms * 4u;
+    // up to 8 resident CTAs per SM (8 x 64 tensor-memory columns = 512)
+    const uint32_t grid = tiles < (uint32_t)sms * 8u ? tiles : (uint32_t)sms * 8u;
     k_linear_fwd_tc<64><<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
         M, K, X, ldx, W, b, Z, ldz, Y, ldy, act, err);
     return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;

@@ -109,8 +109,9 @@ k_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases, uint2* cells,
 }
 
 // r_min / r_max of every case over its particles.  Cases are contiguous
-// runs of particles, so warps are almost always single-case: a warp
-// reduces its lanes and issues one atomic per case it touches.
+// runs of particles, so warps are almost always single-case: a warp reduces
+// its lanes and keeps a running box while its tiles stay in one case,
+// issuing the atomics only when the case changes and at the end.
 template<int D>
 __global__ void __launch_bounds__(256)
 k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
@@ -121,6 +122,19 @@ k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
         return;
     const int lane = threadIdx.x & 31;
     bool bad = false;
+    float wmn[VS], wmx[VS];
+    uint32_t wk = 0xffffffffu;  // case of the running box (warp-uniform)
+    for (int d = 0; d < VS; d++) {
+        wmn[d] = INFINITY;
+        wmx[d] = -INFINITY;
+    }
+    auto flush = [&]() {
+        if (lane == 0 && wk != 0xffffffffu)
+            for (int d = 0; d < VS; d++) {
+                atomic_min_float(&cs[wk].r_min[d], wmn[d]);
+                atomic_max_float(&cs[wk].r_max[d], wmx[d]);
+            }
+    };
     // grid-stride over warp-sized tiles so that a warp's lanes are adjacent
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -151,11 +165,19 @@ k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
                     mx[d] = cl_max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
                 }
             }
-            if (lane == 0 && k0 != 0xffffffffu)
+            if (k0 != wk) {
+                flush();
+                wk = k0;
                 for (int d = 0; d < VS; d++) {
-                    atomic_min_float(&cs[k0].r_min[d], mn[d]);
-                    atomic_max_float(&cs[k0].r_max[d], mx[d]);
+                    wmn[d] = mn[d];
+                    wmx[d] = mx[d];
                 }
+            } else {
+                for (int d = 0; d < VS; d++) {
+                    wmn[d] = cl_min(wmn[d], mn[d]);
+                    wmx[d] = cl_max(wmx[d], mx[d]);
+                }
+            }
         } else if (valid) {
             for (int d = 0; d < VS; d++) {
                 atomic_min_float(&cs[k].r_min[d], mn[d]);
@@ -163,6 +185,7 @@ k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
             }
         }
     }
+    flush();
     if (__any_sync(0xffffffffu, bad) && lane == 0)
         atomicOr(&sc->err, kErrNonFinite);
 }

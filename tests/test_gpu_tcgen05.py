@@ -23,7 +23,7 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("M,K", [(128, 16), (300, 64), (1000, 144), (5000, 80),
-                                 (1, 64)])
+                                 (1, 64), (200000, 64)])
 def test_tcgen05_forward_matches(torch, M, K):
     from aquagpusph_gb300 import learned as Lm
     L = Lm.lib()
