@@ -219,8 +219,12 @@ aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N, const uint16_t* X,
         return AQUA_ERR_INVALID;
     if (M == 0)
         return AQUA_OK;
-    const size_t bytes = ((size_t)N * K * 2 + 1023) / 1024 * 1024 +
-                         (size_t)kTcRows * K * 2;
+    size_t bytes = ((size_t)N * K * 2 + 1023) / 1024 * 1024 +
+                   (size_t)kTcRows * K * 2;
+    // at least 30 KB per CTA keeps <= 7 CTAs on an SM (7 x 64 of the 512
+    // tensor-memory columns), so tcgen05.alloc never has to wait
+    if (bytes < 30 * 1024)
+        bytes = 30 * 1024;
     static bool configured = false;
     if (!configured) {
         if (cudaFuncSetAttribute(k_linear_fwd_tc<64>,
@@ -235,7 +239,6 @@ aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N, const uint16_t* X,
             cudaSuccess)
         return AQUA_ERR_CUDA;
     const uint32_t tiles = (M + kTcRows - 1) / kTcRows;
-    // up to 8 resident CTAs per SM (8 x 64 tensor-memory columns = 512)
     const uint32_t grid = tiles < (uint32_t)sms * 8u ? tiles : (uint32_t)sms * 8u;
     k_linear_fwd_tc<64><<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
         M, K, X, ldx, W, b, Z, ldz, Y, ldy, act, err);
