@@ -62,6 +62,12 @@ def workload(name):
                         "h=0.008 m, c0=25, BIe walls, roll about the bottom "
                         "centre with amplitude U[2,8] deg and period U[1.2,2] s, "
                         f"one probe per tank: N={b.case.N}")
+    if name == "c4":
+        c = cases.dam_break_3d(dx=0.003)
+        c.dt = c.params.dt_fixed
+        return c, ("3-D dam break at dx=0.003 m, h=0.006 m (SPHERIC test-2 tank "
+                   "3.22x1.0x1.0 m, block 1.228x1.0x0.55 m), BIe walls on 5 "
+                   f"faces, 4 probes: N={c.N}")
     if name == "c1s":
         c, _ = cpu_sample("c1")
         return c, ("3-D dam break slab at dx=0.005 m, h=0.01 m (tank "
@@ -94,6 +100,12 @@ def cpu_sample(name):
         b = cases.sloshing_batch_2d()
         return b, (f"the whole batch (64 tanks, N={b.case.N}), each tank "
                    "stepped by the oracle in turn")
+    if name == "c4":
+        c = cases.dam_break_3d(dx=0.003, tank=(0.48, 0.12, 0.36),
+                               block=(0.24, 0.12, 0.33), probes_z=(0.02,))
+        c.dt = c.params.dt_fixed
+        return c, ("3-D dam break slab at the workload's dx=0.003 m / h=0.006 m: "
+                   f"tank 0.48x0.12x0.36 m, block 0.24x0.12x0.33 m, N={c.N}")
     if name in ("c1s", "c1m"):
         name = "c1"
     if name == "c0":
@@ -197,6 +209,25 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(x: float, world: int) -> float:
+    """The largest value over the ranks: the job takes as long as its
+    slowest replica."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world: int, n_per_rank: int, steps: int, seconds: float) -> float:
+    """Particle-steps/s of the whole job: every rank advances its own replica
+    of the workload (weak scaling)."""
+    return world * n_per_rank * steps / seconds
+
+
 # DRAM bytes per particle of the fused sweep from one ncu capture of the
 # 1.89M-particle profiling case (dram__bytes_read.sum + dram__bytes_write.sum
 # over N; profiles/k_sweep_c1m.md), scaled to a launch by N.
@@ -235,6 +266,8 @@ def run_reference(args):
 def workload_desc(name):
     if name in ("c2", "c3"):
         return "batched 2-D sloshing, 64 tanks, dx=0.004 m (N=935,414)"
+    if name == "c4":
+        return "3-D dam break, SPHERIC test-2 geometry at dx=0.003 m (~25M particles)"
     if name == "c1m":
         return "3-D dam break, 1.6x0.5x0.6 m tank, dx=0.005 m"
     if name == "c1s":
@@ -299,14 +332,9 @@ def run_ours(args):
     clk = clocks.stop()
     sv.check(stream=sid)
     sc = sv.scalars(stream=sid)
+    ms_total = max_over_ranks(ms_total, world)
     ms_step = ms_total / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
-        ms_step = ms_total / args.steps
-    value = world * c.N * args.steps / (ms_total * 1e-3)
+    value = job_throughput(world, c.N, args.steps, ms_total * 1e-3)
 
     # ---- the other arithmetic build of the same step, same workload
     other = "exact" if args.precision == "fast" else "fast"
@@ -361,13 +389,9 @@ def run_ours(args):
     stream.synchronize()
     e2e_s = time.perf_counter() - t0
     barrier()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world)
     sv.check(stream=sid)
-    e2e_value = world * c.N * e2e_steps / e2e_s
+    e2e_value = job_throughput(world, c.N, e2e_steps, e2e_s)
 
     # ---- roofline of the dominant kernel (the fused sweep)
     peaks = {}
@@ -625,7 +649,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c1",
-                    choices=["c1", "c0", "c1s", "c1m", "c2", "c3"])
+                    choices=["c1", "c0", "c1s", "c1m", "c2", "c3", "c4"])
     ap.add_argument("--train-pairs", type=int, default=24)
     ap.add_argument("--train-iters", type=int, default=300)
     ap.add_argument("--eval-warm", type=int, default=3000)
