@@ -73,6 +73,9 @@ class Params:
     min_bound_dist: float = 0.0
     relax_midpoint: float = 0.0
     iter_midpoint_max: int = 1
+    # wall formulation: 0 = BIe (canonical), 1 = BI (analytic Shepard,
+    # free-slip boundary integrals)
+    boundary: int = 0
 
     # compiled Definitions (CalcServer.cpp:235-264, basic.xml:118-129)
     @property

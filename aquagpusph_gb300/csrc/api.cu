@@ -95,6 +95,8 @@ build_consts(const aqua_params* p, Consts& c)
         return AQUA_ERR_INVALID;
     if (p->iter_midpoint_max != 1)
         return AQUA_ERR_INVALID;  // one midpoint iteration (canonical stack)
+    if (p->boundary != AQUA_BOUNDARY_BIE && p->boundary != AQUA_BOUNDARY_BI)
+        return AQUA_ERR_INVALID;
     std::memset(&c, 0, sizeof(c));
     c.dims = p->dims;
     c.n_sets = p->n_sets;
@@ -118,6 +120,7 @@ build_consts(const aqua_params* p, Consts& c)
     c.min_bound_dist = p->min_bound_dist;
     c.relax_midpoint = p->relax_midpoint;
     c.iter_midpoint_max = p->iter_midpoint_max;
+    c.boundary = p->boundary;
     for (uint32_t k = 0; k < p->n_sets; k++) {
         c.refd[k] = p->refd[k];
         c.visc_dyn[k] = p->visc_dyn[k];
@@ -277,6 +280,12 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
         AQ_CUDA(launch_gather<3>(x->fast, x->consts, a, s));
     else
         AQ_CUDA(launch_gather<2>(x->fast, x->consts, a, s));
+    if (x->consts.boundary == AQUA_BOUNDARY_BI) {
+        if (x->dims == 3)
+            AQ_CUDA(launch_bi_walls<3>(x->fast, x->consts, a, s));
+        else
+            AQ_CUDA(launch_bi_walls<2>(x->fast, x->consts, a, s));
+    }
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[2], s, cudaEventRecordExternal));
     if (x->dims == 3)
@@ -912,8 +921,11 @@ aqua_launches_per_step(aqua_ctx* x)
     if (!x)
         return 0;
     // begin, minmax, ncells, icell+hist, (passes - 1) hist,
-    // passes x (scan, scatter), gather, chunks, sweep, finalize [, motion]
-    return 4u + (x->passes - 1u) + 2u * x->passes + 4u + (x->has_motion ? 1u : 0u);
+    // passes x (scan, scatter), gather, [BI walls,] chunks, sweep, finalize
+    // [, motion]
+    return 4u + (x->passes - 1u) + 2u * x->passes + 4u +
+           (x->consts.boundary == AQUA_BOUNDARY_BI ? 1u : 0u) +
+           (x->has_motion ? 1u : 0u);
 }
 
 }  // extern "C"

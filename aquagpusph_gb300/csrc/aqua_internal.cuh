@@ -40,6 +40,7 @@ struct Consts
     float dr_factor, min_bound_dist, relax_midpoint;
     uint32_t iter_midpoint_max;
     float refd[kMaxSets], visc_dyn[kMaxSets], delta[kMaxSets];
+    int boundary;       // AQUA_BOUNDARY_BIE or AQUA_BOUNDARY_BI
     // derived
     float cell_length;  // support * h (LinkList.cpp:156)
     float idist;        // 1 / (support * h) (LinkList.cl.in:73)

@@ -142,7 +142,13 @@ cudaError_t launch_free_surface(int dims, const float* r, const int32_t* imove,
                                 uint32_t n_sensors, float dr, int* keys,
                                 float* out, cudaStream_t s);
 
+template<int D>
+cudaError_t launch_bi_walls(bool fast, const Consts& c, const StepArgs& a,
+                            cudaStream_t s);
+
 namespace exact {
+template<int D>
+cudaError_t launch_bi_walls_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
 template<int D>
 cudaError_t launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
 template<int D>
@@ -150,6 +156,8 @@ cudaError_t launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
                               int variant, cudaStream_t s);
 }  // namespace exact
 namespace fast {
+template<int D>
+cudaError_t launch_bi_walls_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
 template<int D>
 cudaError_t launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
 template<int D>

@@ -206,6 +206,14 @@ launch_sweep(bool fast, const Consts& c, const StepArgs& a, unsigned grid,
                 : exact::launch_sweep_impl<D>(c, a, grid, variant, s);
 }
 
+template<int D>
+cudaError_t
+launch_bi_walls(bool fast, const Consts& c, const StepArgs& a, cudaStream_t s)
+{
+    return fast ? fast::launch_bi_walls_impl<D>(c, a, s)
+                : exact::launch_bi_walls_impl<D>(c, a, s);
+}
+
 cudaError_t
 launch_finalize(DevScalars* sc, CaseScalars* cs, const CaseMotion* cm,
                 uint32_t n_cases, cudaStream_t s)
@@ -243,6 +251,10 @@ launch_export_ihoc(const uint2* cells, uint32_t* ihoc, uint32_t ncap,
     return cudaGetLastError();
 }
 
+template cudaError_t launch_bi_walls<2>(bool, const Consts&, const StepArgs&,
+                                        cudaStream_t);
+template cudaError_t launch_bi_walls<3>(bool, const Consts&, const StepArgs&,
+                                        cudaStream_t);
 template cudaError_t launch_motion<2>(const StepArgs&, cudaStream_t);
 template cudaError_t launch_motion<3>(const StepArgs&, cudaStream_t);
 template cudaError_t launch_gather<2>(bool, const Consts&, const StepArgs&, cudaStream_t);

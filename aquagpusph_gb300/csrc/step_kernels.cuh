@@ -82,6 +82,65 @@ kernel_f(float q)
     return f * a;
 }
 
+// Boundary-integral Shepard factor (KernelFunctions/Wendland{2D,3D}.hcl:
+// kernelS_P, the polynomial part, and kernelS_D, the analytic part)
+template<int D>
+__device__ __forceinline__ float
+kernel_sp(float q)
+{
+    const float q2 = q * q;
+    const float q3 = q2 * q;
+    if (D == 3) {
+        constexpr float wcon = 0.08203125f * 0.318309886f;
+        return wcon * (0.25f * q3 * q2 - 2.142857f * q2 * q2 + 6.666667f * q3 -
+                       8.f * q2 + 5.333333f);
+    } else {
+        constexpr float wcon = 0.109375f * 0.318309886f;
+        return wcon * (0.285714f * q3 * q2 - 2.5f * q2 * q2 + 8.f * q3 -
+                       10.f * q2 + 8.f);
+    }
+}
+
+__device__ __forceinline__ float
+acospi_f(float x)
+{
+    return acosf(x) / 3.14159265f;
+}
+
+__device__ __forceinline__ float
+omega_f(float a, float b)
+{
+    const float a2 = a * a;
+    const float b2 = b * b;
+    const float v = sqrtf((1.f + a2 + b2) / ((1.f + a2) * (1.f + b2)));
+    return acospi_f((1.f < v) ? 1.f : v);
+}
+
+__device__ __forceinline__ float
+sign_f(float x)
+{
+    return (x > 0.f) ? 1.f : ((x < 0.f) ? -1.f : 0.f);
+}
+
+template<int D>
+__device__ __forceinline__ float
+kernel_sd(float d, float t, float b, float s)
+{
+    if (D == 3) {
+        const float wcon = 0.25f;
+        const float dr = 0.5f * sqrtf(s);
+        const float t1 = (t - dr) / d, t2 = (t + dr) / d;
+        const float b1 = (b - dr) / d, b2 = (b + dr) / d;
+        const float st = sign_f(t1), sb = sign_f(b1);
+        return -wcon * (omega_f(t2, b2) - st * omega_f(t1, b2) -
+                        sb * omega_f(t2, b1) + st * sb * omega_f(t1, b1));
+    } else {
+        constexpr float wcon = 0.5f * 0.318309886f;
+        const float dr = 0.5f * s;
+        return -wcon * (atanf((t + dr) / d) - atanf((t - dr) / d));
+    }
+}
+
 __device__ __forceinline__ float
 cl_min(float x, float y)
 {
@@ -285,7 +344,7 @@ k_gather(Consts c, StepArgs a)
 // neighbour cells of the warp's cell.  The scan checks the queues every 32
 // candidates, where they have room for at least 32 more, so a queue never
 // overflows.
-template<int D, int NT, int NQ, typename QE, bool BULK>
+template<int D, int NT, int NQ, typename QE, bool BULK, bool BI>
 __device__ __forceinline__ float
 sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                QE* queue, uint32_t* cstart, float4* grp2, uint64_t* mbar,
@@ -303,7 +362,12 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     const uint32_t nxy = cas.n_cells[0] * cas.n_cells[1];
     const uint32_t key_i = a.skeys[i];
     const bool fluid = valid && (im == 1), sensor = valid && (im == 0);
-    const bool want_shep = valid && (im >= -3) && (im <= 1);
+    // BIe: the Shepard sum runs for -3 <= imove <= 1 (cfd/Shepard.cl); BI:
+    // the walls are handled by k_bi_walls, fluid and probes take fluid
+    // neighbours only here and the walls in the epilogue
+    constexpr bool bie = !BI;  // the wall formulation is a compile-time choice
+    const bool want_shep = valid && (bie ? (im >= -3) && (im <= 1)
+                                         : (im == 0) || (im == 1));
 
     float shep = 0.f;
     float gp[3] = { 0.f, 0.f, 0.f }, lu[3] = { 0.f, 0.f, 0.f };
@@ -539,7 +603,8 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                 const float d2 = pj.z - ri[2];
                 rr = rr + d2 * d2;
             }
-            const bool take = want_shep && (jm == 1 || (fluid && jm == -3)) &&
+            const bool take = want_shep &&
+                              (jm == 1 || (bie && fluid && jm == -3)) &&
                               rr < c.q2_reject;
             if (take) {
                 if constexpr (sizeof(QE) == 2)
@@ -573,13 +638,76 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     drain(qt);
     if (!valid)
         return INFINITY;
+    if constexpr (BI) {
+        // BI walls: the analytic Shepard factor (BI/Shepard.cl compute) of
+        // fluid particles and probes, and the wall terms of the fluid
+        // particles (BI/Interactions.cl) added onto the completed fluid
+        // sums, walls in visiting order
+        if (im == -3)
+            return c.dt_fixed;  // done by k_bi_walls
+        shep = 1.f;
+        bool self_added = false;
+        for (int k = 0; k < NC; k++) {
+            const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
+            if (!a.b.cell_wall[cn])
+                continue;
+            const uint2 se = a.b.cells[cn];
+            for (uint32_t j = se.x; j < se.y; j++) {
+                const float4 pj = a.b.posq[j];
+                if (__float_as_int(pj.w) != -3)
+                    continue;
+                float d[3];
+                d[0] = pj.x - ri[0];
+                d[1] = pj.y - ri[1];
+                d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
+                const float q = sqrtf(dot_d<D>(d, d)) / c.H;
+                if (q >= c.SUPPORT)
+                    continue;
+                float nj[3], tj[3], bj[3];
+                load_normal<D>(a.dst.normal, j, nj);
+                load_normal<D>(a.dst.tangent, j, tj);
+                load_normal<D>(a.dst.binormal, j, bj);
+                const float area = a.b.pmq[j].y;
+                const float rn = dot_d<D>(d, nj);
+                if ((rn > -1e-8f * c.H) && (rn < 1e-8f * c.H)) {
+                    if (!self_added) {
+                        const float rt = fabsf(dot_d<D>(d, tj));
+                        const float rb = fabsf(dot_d<D>(d, bj));
+                        const float dr = 0.55f * powf(area, 1.f / (c.DIMS - 1.f));
+                        if ((rt <= dr) && (rb <= dr)) {
+                            self_added = true;
+                            shep = shep - 0.5f;
+                        }
+                    }
+                } else {
+                    const float rt = fabsf(dot_d<D>(d, tj));
+                    const float rb = fabsf(dot_d<D>(d, bj));
+                    shep = shep + (rn * c.CONW * kernel_sp<D>(q) * area +
+                                   kernel_sd<D>(fabsf(rn), rt, rb, area));
+                }
+                if (fluid) {
+                    const float pw = a.b.pmq[j].x;
+                    const float4 vw = a.b.velq[j];
+                    const float w = kernel_w<D>(q) * c.CONW * area;
+                    const float sg = (p_i + pw) / rho_i * w;
+                    for (int kk = 0; kk < D; kk++)
+                        gp[kk] = gp[kk] + sg * nj[kk];
+                    float dv[3];
+                    dv[0] = vw.x - uiv[0];
+                    dv[1] = vw.y - uiv[1];
+                    dv[2] = (D == 3) ? vw.z - uiv[2] : 0.f;
+                    du = du + rho_i * dot_d<D>(dv, nj) * w;
+                }
+            }
+        }
+    }
     if (a.b.shepard)
         a.b.shepard[i] = want_shep ? shep : 0.f;
 
     float gpf[4] = { 0.f, 0.f, 0.f, 0.f }, luf[4] = { 0.f, 0.f, 0.f, 0.f };
     float gwf[4] = { 0.f, 0.f, 0.f, 0.f };
     float div_u = 0.f;
-    if (fluid) {
+    if (fluid && bie) {
         for (int k = 0; k < D; k++) {
             gpf[k] = gp[k];
             luf[k] = lu[k];
@@ -590,6 +718,17 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         for (int k = 0; k < VS; k++)
             gpf[k] = gpf[k] + s2 * gwf[k];
         div_u = du - 2.f * rho_i * (dot_full<D>(ui_full, gwf) + dbi);
+    } else if (fluid) {
+        // BI/Shepard.cl apply: renormalise by the analytic Shepard factor
+        for (int k = 0; k < D; k++) {
+            gpf[k] = gp[k];
+            luf[k] = lu[k];
+        }
+        for (int k = 0; k < VS; k++) {
+            gpf[k] = gpf[k] / shep;
+            luf[k] = luf[k] / shep;
+        }
+        div_u = du / shep;
     }
     if (a.extras) {
         Vec<D>::store(a.b.grad_p, i, gpf);
@@ -637,7 +776,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         const float delta_f = c.delta[set] * dt * rho_i / c.refd[set];
         drhodt = drhodt + delta_f * lp;
         // BIe ElasticBounce.cl
-        if (dt != 0.f) {
+        if (bie && dt != 0.f) {
             float vh[3];
             for (int k = 0; k < D; k++)
                 vh[k] = uin[k] + hdt * acc[k];
@@ -704,7 +843,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     }
     const float rho_n = a.b.rho_in[i] + dt * drhodt;
     // BIe PST.cl
-    if (fluid) {
+    if (fluid && bie) {
         const float Ri = 0.5f * powf(T.m[i] / rho_n, 1.f / c.DIMS);
         for (int k = 0; k < NC; k++) {
             const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
@@ -749,8 +888,9 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
 
 // Persistent sweep: warps fetch cell-aligned chunks of <= 32 particles
 // NT threads per block, NQ queued neighbours per thread (power of 2, >= 64)
-// of type QE, candidate groups copied by the bulk-copy engine when BULK
-template<int D, int NT, int NQ, typename QE, bool BULK>
+// of type QE, candidate groups copied by the bulk-copy engine when BULK,
+// BI walls (cfd/BI.xml) when BI, else BIe walls
+template<int D, int NT, int NQ, typename QE, bool BULK, bool BI>
 __global__ void __launch_bounds__(NT, 640 / NT)
 k_sweep(Consts c, StepArgs a)
 {
@@ -789,7 +929,7 @@ k_sweep(Consts c, StepArgs a)
                 break;
             const uint2 cw = a.b.chunks[ch];
             const bool valid = (uint32_t)lane < cw.y;
-            float v = sweep_particle<D, NT, NQ, QE, BULK>(
+            float v = sweep_particle<D, NT, NQ, QE, BULK, BI>(
                 c, a, valid ? cw.x + lane : cw.x, valid, s_queue + threadIdx.x,
                 s_cstart[warp], s_grp[warp], s_mbar[warp], phases);
             __syncwarp();  // s_cstart and s_grp are rewritten for the next chunk
@@ -805,6 +945,151 @@ k_sweep(Consts c, StepArgs a)
         }
     }
     flush();
+}
+
+// BI walls before the sweep (cfd/BI.xml): for every boundary element, its
+// analytic Shepard factor (BI/Shepard.cl compute: the other elements of the
+// support), the free-slip Laplacian of the fluid velocity (BI/LapU.cl), the
+// pressure gradient it implies (BI/GradP.cl), the pressure interpolated
+// from the fluid (BI/Interpolation.cl, a second pass: it needs that
+// gradient) and its Shepard renormalisation with the density from the
+// linear EOS (BI/InterpolationShepard.cl).  The sweep then reads the
+// elements' pressure from the packed records.
+template<int D>
+__global__ void __launch_bounds__(128)
+k_bi_walls(Consts c, StepArgs a)
+{
+    constexpr int VS = Vec<D>::VS;
+    constexpr int NC = (D == 3) ? 27 : 9;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.N || a.sc->err)
+        return;
+    const float4 pi = a.b.posq[i];
+    if (__float_as_int(pi.w) != -3)
+        return;
+    const VarSet& T = a.dst;
+    const CaseScalars& cas = a.cs[T.cid[i]];
+    const uint32_t nx = cas.n_cells[0];
+    const uint32_t nxy = cas.n_cells[0] * cas.n_cells[1];
+    const uint32_t key_i = a.skeys[i];
+    const float ri[3] = { pi.x, pi.y, pi.z };
+    const float4 vi = a.b.velq[i];
+    const float ui[3] = { vi.x, vi.y, vi.z };
+    float shep = 1.f;
+    bool self_added = false;
+    float lap[4] = { 0.f, 0.f, 0.f, 0.f };
+    for (int k = 0; k < NC; k++) {
+        const uint2 se = a.b.cells[neighbour_cell<D>(key_i, k, nx, nxy)];
+        for (uint32_t j = se.x; j < se.y; j++) {
+            const float4 pj = a.b.posq[j];
+            const int jm = __float_as_int(pj.w);
+            if (jm == -3) {
+                if (j == i) {
+                    if (!self_added) {
+                        self_added = true;
+                        shep = shep - 0.5f;
+                    }
+                    continue;
+                }
+            } else if (jm != 1) {
+                continue;
+            }
+            float d[3];
+            d[0] = pj.x - ri[0];
+            d[1] = pj.y - ri[1];
+            d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
+            const float q = sqrtf(dot_d<D>(d, d)) / c.H;
+            if (q >= c.SUPPORT)
+                continue;
+            if (jm == 1) {
+                const float4 vj = a.b.velq[j];
+                const float f = kernel_f<D>(q) * c.CONF * a.b.pmq[j].y;
+                const float s2 = f * 2.f / vj.w;
+                lap[0] = lap[0] + s2 * (vj.x - ui[0]);
+                lap[1] = lap[1] + s2 * (vj.y - ui[1]);
+                if (D == 3)
+                    lap[2] = lap[2] + s2 * (vj.z - ui[2]);
+                continue;
+            }
+            float nj[3], tj[3], bj[3];
+            load_normal<D>(T.normal, j, nj);
+            load_normal<D>(T.tangent, j, tj);
+            load_normal<D>(T.binormal, j, bj);
+            const float area = a.b.pmq[j].y;
+            const float rn = dot_d<D>(d, nj);
+            if ((rn > -1e-8f * c.H) && (rn < 1e-8f * c.H)) {
+                if (!self_added) {
+                    const float rt = fabsf(dot_d<D>(d, tj));
+                    const float rb = fabsf(dot_d<D>(d, bj));
+                    const float dr = 0.55f * powf(area, 1.f / (c.DIMS - 1.f));
+                    if ((rt <= dr) && (rb <= dr)) {
+                        self_added = true;
+                        shep = shep - 0.5f;
+                    }
+                }
+                continue;
+            }
+            const float rt = fabsf(dot_d<D>(d, tj));
+            const float rb = fabsf(dot_d<D>(d, bj));
+            shep = shep + (rn * c.CONW * kernel_sp<D>(q) * area +
+                           kernel_sd<D>(fabsf(rn), rt, rb, area));
+        }
+    }
+    // BI/GradP.cl freeslip
+    const uint32_t set_raw = T.iset[i];
+    const uint32_t set = set_raw < c.n_sets ? set_raw : 0u;
+    const float sh = shep < 1.0e-6f ? 1.f : shep;
+    float dudt[4];
+    Vec<D>::load(a.b.dudt_in, i, dudt);
+    float gw[4];
+    for (int k = 0; k < VS; k++)
+        gw[k] = c.visc_dyn[set] / c.refd[set] * lap[k] / sh + c.g[k] - dudt[k];
+    // BI/Interpolation.cl
+    const float rho_i = vi.w;
+    float gpi[3];
+    for (int k = 0; k < 3; k++)
+        gpi[k] = rho_i * gw[k];
+    float p = 0.f;
+    for (int k = 0; k < NC; k++) {
+        const uint2 se = a.b.cells[neighbour_cell<D>(key_i, k, nx, nxy)];
+        for (uint32_t j = se.x; j < se.y; j++) {
+            const float4 pj = a.b.posq[j];
+            if (__float_as_int(pj.w) != 1)
+                continue;
+            float d[3];
+            d[0] = pj.x - ri[0];
+            d[1] = pj.y - ri[1];
+            d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
+            const float q = sqrtf(dot_d<D>(d, d)) / c.H;
+            if (q >= c.SUPPORT)
+                continue;
+            const float2 pm = a.b.pmq[j];
+            const float w = kernel_w<D>(q) * c.CONW * pm.y / a.b.velq[j].w;
+            p = p + (pm.x - dot_d<D>(gpi, d)) * w;
+        }
+    }
+    // BI/InterpolationShepard.cl
+    p = p / sh;
+    const float rho = c.refd[set] + (p - c.p0) / (c.cs * c.cs);
+    T.p[i] = p;
+    T.rho[i] = rho;
+    a.b.pmq[i].x = p;
+    if (a.b.shepard)
+        a.b.shepard[i] = shep;
+    if (a.extras) {
+        Vec<D>::store(a.b.lap_u, i, lap);
+        Vec<D>::store(a.b.grad_p, i, gw);
+    }
+}
+
+template<int D>
+cudaError_t
+launch_bi_walls_impl(const Consts& c, const StepArgs& a, cudaStream_t s)
+{
+    if (a.N == 0)
+        return cudaSuccess;
+    k_bi_walls<D><<<(a.N + 127) / 128, 128, 0, s>>>(c, a);
+    return cudaGetLastError();
 }
 
 template<int D>
@@ -827,26 +1112,33 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
 {
     if (a.N == 0)
         return cudaSuccess;
+    if (c.boundary == AQUA_BOUNDARY_BI) {
+        // one launch shape for the BI walls
+        k_sweep<D, 64, 128, uint16_t, false, true><<<grid, 64, 0, s>>>(c, a);
+        return cudaGetLastError();
+    }
     switch (variant) {
     case 1:
-        k_sweep<D, 64, 128, uint16_t, false><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 128, uint16_t, false, false><<<grid, 64, 0, s>>>(c, a);
         break;
     case 2:
-        k_sweep<D, 64, 64, uint32_t, false><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 64, uint32_t, false, false><<<grid, 64, 0, s>>>(c, a);
         break;
     case 3:
-        k_sweep<D, 64, 128, uint16_t, true><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 128, uint16_t, true, false><<<grid, 64, 0, s>>>(c, a);
         break;
     case 4:
-        k_sweep<D, 64, 64, uint32_t, true><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 64, uint32_t, true, false><<<grid, 64, 0, s>>>(c, a);
         break;
     default:
-        k_sweep<D, 128, 128, uint16_t, false><<<grid, 128, 0, s>>>(c, a);
+        k_sweep<D, 128, 128, uint16_t, false, false><<<grid, 128, 0, s>>>(c, a);
         break;
     }
     return cudaGetLastError();
 }
 
+template cudaError_t launch_bi_walls_impl<2>(const Consts&, const StepArgs&, cudaStream_t);
+template cudaError_t launch_bi_walls_impl<3>(const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_gather_impl<2>(const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_gather_impl<3>(const Consts&, const StepArgs&, cudaStream_t);
 template cudaError_t launch_sweep_impl<2>(const Consts&, const StepArgs&, unsigned,

@@ -82,7 +82,14 @@ typedef struct
     const float* refd;         /* host, n_sets: per-set reference density */
     const float* visc_dyn;     /* host, n_sets: dynamic viscosity */
     const float* delta;        /* host, n_sets: delta-SPH factor */
+    int32_t boundary;          /* wall formulation: AQUA_BOUNDARY_BIE (the
+                                  canonical cfd/BIe.xml) or AQUA_BOUNDARY_BI
+                                  (cfd/BI.xml: analytic Shepard factor,
+                                  free-slip boundary integrals) */
 } aqua_params;
+
+#define AQUA_BOUNDARY_BIE 0
+#define AQUA_BOUNDARY_BI 1
 
 /* The particle Variables of one case (all length N; pointers may be host or
  * device memory as each function states).  Fields a call does not use may

@@ -808,6 +808,8 @@ aq_linklist(aq_state* st, const aq_params* pr, int nthreads)
 {
     if (!st || !pr || !st->N)
         return AQ_ERR_INVALID;
+    if (pr->boundary != 0)
+        return AQ_ERR_INVALID;  // BI walls: only the reference-kernel harness
     if (pr->dims == 3) {
         Case<3> cs{ st, pr, threads(nthreads), st->N };
         return linklist<3>(cs);

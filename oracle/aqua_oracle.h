@@ -55,6 +55,9 @@ typedef struct
     const float* refd;
     const float* visc_dyn;
     const float* delta;
+    /* wall formulation: 0 = BIe (cfd/BIe.xml, the canonical stack), 1 = BI
+     * (cfd/BI.xml: analytic Shepard, free-slip boundary integrals) */
+    int32_t boundary;
     /* prescribed roll of the boundary elements and probes (non-fluid
      * particles of set roll_iset) about z through roll_center:
      * psi(t) = roll_amplitude * sin(roll_angular_freq * t), applied after the

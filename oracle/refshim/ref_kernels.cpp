@@ -12,7 +12,8 @@
  * cannot be compiled here), restated:
  *   - the preset tool order of one step, basic.xml:132-171 as modified by
  *     basic/time_scheme/midpoint.xml, basic/domain.xml, cfd.xml,
- *     cfd/deltaSPH.xml, cfd/BIe.xml and cfd/variableTimeStep.xml;
+ *     cfd/deltaSPH.xml, cfd/BIe.xml and cfd/variableTimeStep.xml, or with
+ *     cfd/BI.xml in place of cfd/BIe.xml (boundary = 1);
  *   - the link-list host logic, LinkList.cpp:185-232 (n_cells, float
  *     division by support*h) and LinkList.cpp:326-494 (tool sequence);
  *   - the radix-sort tool as the stable sort it is (RadixSort.cpp:130-304,
@@ -133,6 +134,30 @@ namespace ref_pst {
 namespace ref_timestep {
 #include "resources/Scripts/cfd/TimeStep.cl"
 }
+/* BI walls (cfd/BI.xml) */
+namespace ref_bi_shepard {
+#include "resources/Scripts/cfd/Boundary/BI/Shepard.cl"
+}
+#undef _SHEPARD_
+namespace ref_bi_lapu {
+#include "resources/Scripts/cfd/Boundary/BI/LapU.cl"
+}
+#undef _LAPU_
+namespace ref_bi_gradp {
+#include "resources/Scripts/cfd/Boundary/BI/GradP.cl"
+}
+namespace ref_bi_interp {
+#include "resources/Scripts/cfd/Boundary/BI/Interpolation.cl"
+}
+#undef _P_
+namespace ref_bi_interp_shepard {
+#include "resources/Scripts/cfd/Boundary/BI/InterpolationShepard.cl"
+}
+namespace ref_bi_interactions {
+#include "resources/Scripts/cfd/Boundary/BI/Interactions.cl"
+}
+#undef _GRADP_
+#undef _DIVU_
 namespace ref_linklist {
 #include "aquagpusph/CalcServer/LinkList.cl.in"
 }
@@ -328,6 +353,13 @@ aq_step(aq_state* st, const aq_params* pr, int nthreads)
         return err;
     const usize4 n_cells = ncells_of(st);
     const usize* icell = w.icell.data();
+    const bool bi = pr->boundary == 1;
+    /* 32-bit copies for the kernel that declares uint link-list arguments
+     * (BI/Interactions.cl) */
+    std::vector<uint> icell32(w.icell.begin(), w.icell.end());
+    std::vector<uint> ihoc32(w.ihoc.begin(), w.ihoc.end());
+    const uint4 n_cells32{ (uint)n_cells.x, (uint)n_cells.y, (uint)n_cells.z,
+                           (uint)n_cells.w };
     const usize* ihoc = w.ihoc.data();
     /* Backup id, iset, imove, normal, tangent, m (basic.xml:141-146) */
     w.id.resize(N);
@@ -385,10 +417,19 @@ aq_step(aq_state* st, const aq_params* pr, int nthreads)
         });
         /* neighbour sweeps; LOCAL_MEM semantics: sums start at zero */
         std::fill(st->shepard, st->shepard + N, 0.f);
-        ndrange(N, nt, [&]() {
-            ref_shepard::entry(st->imove, r, st->rho, st->m, st->shepard, N,
-                               icell, ihoc, n_cells);
-        });
+        if (bi) {
+            /* cfd Shepard replaced by the analytic BI factor (BI.xml:33) */
+            ndrange(N, nt, [&]() {
+                ref_bi_shepard::compute(st->imove, r, normal, tangent, binormal,
+                                        st->m, st->shepard, N, icell, ihoc,
+                                        n_cells);
+            });
+        } else {
+            ndrange(N, nt, [&]() {
+                ref_shepard::entry(st->imove, r, st->rho, st->m, st->shepard, N,
+                                   icell, ihoc, n_cells);
+            });
+        }
         std::fill(grad_p, grad_p + N, VEC_ZERO);
         std::fill(lap_u, lap_u + N, VEC_ZERO);
         std::fill(st->div_u, st->div_u + N, 0.f);
@@ -410,17 +451,50 @@ aq_step(aq_state* st, const aq_params* pr, int nthreads)
             ref_deltasph::lapp(st->imove, r, st->rho, st->m, st->p, st->lap_p,
                                N, icell, ihoc, n_cells);
         });
-        std::fill(grad_w_bi, grad_w_bi + N, VEC_ZERO);
-        std::fill(st->div_u_bi, st->div_u_bi + N, 0.f);
-        ndrange(N, nt, [&]() {
-            ref_bie_interactions::entry(st->imove, r, normal, u, st->m,
-                                        grad_w_bi, st->div_u_bi, N, icell,
-                                        ihoc, n_cells);
-        });
-        ndrange(N, nt, [&]() {
-            ref_bie_rates::entry(st->imove, st->rho, st->p, u, grad_w_bi,
-                                 st->div_u_bi, grad_p, st->div_u, N);
-        });
+        if (bi) {
+            /* BI.xml:24-32, in insertion order before "Interactions" */
+            ndrange(N, nt, [&]() {
+                ref_bi_lapu::freeslip(st->imove, r, u, st->rho, st->m, lap_u,
+                                      N, icell, ihoc, n_cells);
+            });
+            ndrange(N, nt, [&]() {
+                ref_bi_gradp::freeslip(st->iset, st->imove, st->shepard,
+                                       st->rho, lap_u, dudt, grad_p,
+                                       pr->visc_dyn, pr->refd, N, g);
+            });
+            ndrange(N, nt, [&]() {
+                ref_bi_interp::entry(st->iset, st->imove, r, st->m, st->rho,
+                                     grad_p, st->p, pr->refd, N, icell, ihoc,
+                                     n_cells);
+            });
+            ndrange(N, nt, [&]() {
+                ref_bi_interp_shepard::entry(st->iset, st->imove, st->shepard,
+                                             st->rho, st->p, pr->refd, N,
+                                             pr->cs, pr->p0);
+            });
+            ndrange(N, nt, [&]() {
+                ref_bi_interactions::entry(st->iset, st->imove, r, normal, u,
+                                           st->rho, st->m, st->p, pr->refd,
+                                           grad_p, st->div_u, icell32.data(),
+                                           ihoc32.data(), N, n_cells32, g);
+            });
+            ndrange(N, nt, [&]() {
+                ref_bi_shepard::apply(st->imove, st->shepard, grad_p, lap_u,
+                                      st->div_u, N, pr->cs);
+            });
+        } else {
+            std::fill(grad_w_bi, grad_w_bi + N, VEC_ZERO);
+            std::fill(st->div_u_bi, st->div_u_bi + N, 0.f);
+            ndrange(N, nt, [&]() {
+                ref_bie_interactions::entry(st->imove, r, normal, u, st->m,
+                                            grad_w_bi, st->div_u_bi, N, icell,
+                                            ihoc, n_cells);
+            });
+            ndrange(N, nt, [&]() {
+                ref_bie_rates::entry(st->imove, st->rho, st->p, u, grad_w_bi,
+                                     st->div_u_bi, grad_p, st->div_u, N);
+            });
+        }
         ndrange(N, nt, [&]() {
             ref_rates::entry(st->iset, st->imove, st->rho, grad_p, lap_u,
                              st->div_u, dudt, st->drhodt, pr->visc_dyn, N, g);
@@ -429,10 +503,12 @@ aq_step(aq_state* st, const aq_params* pr, int nthreads)
             ref_deltasph::deltaSPH(st->iset, st->imove, st->rho, st->lap_p,
                                    st->drhodt, pr->refd, pr->delta, N, dt);
         });
-        ndrange(N, nt, [&]() {
-            ref_elastic_bounce::entry(st->imove, r_in, normal, st->m, u_in,
-                                      dudt, N, dt, icell, ihoc, n_cells);
-        });
+        if (!bi) {
+            ndrange(N, nt, [&]() {
+                ref_elastic_bounce::entry(st->imove, r_in, normal, st->m, u_in,
+                                          dudt, N, dt, icell, ihoc, n_cells);
+            });
+        }
         ndrange(N, nt, [&]() {
             ref_midpoint::relax(st->imove, dudt_in, dudt, st->drhodt_in,
                                 st->drhodt, N, pr->relax_midpoint);
@@ -443,10 +519,12 @@ aq_step(aq_state* st, const aq_params* pr, int nthreads)
         ref_midpoint::corrector(st->imove, r_in, r, u_in, u, dudt, st->rho_in,
                                 st->rho, st->drhodt, N, dt);
     });
-    ndrange(N, nt, [&]() {
-        ref_pst::entry(st->imove, r, normal, st->m, st->rho, N, icell, ihoc,
-                       n_cells);
-    });
+    if (!bi) {
+        ndrange(N, nt, [&]() {
+            ref_pst::entry(st->imove, r, normal, st->m, st->rho, N, icell,
+                           ihoc, n_cells);
+        });
+    }
     /* fixed time step, variable time step, minimum time step (reduction) */
     const float dt_fixed = pr->dt_fixed;
     ndrange(N, nt, [&]() {

@@ -101,6 +101,7 @@ struct usize2 { usize x, y; };
 struct usize3 { usize x, y, z; };
 struct usize4 { usize x, y, z, w; };
 struct uint4 { uint x, y, z, w; };
+#define uivec4 uint4
 
 /* ------------------------------------------------------ element-wise ops */
 #define F2_BIN(OP) float2(a.x OP b.x, a.y OP b.y)
@@ -169,10 +170,11 @@ inline float pow(float x, float y) { return std::pow(x, y); }
 inline float fabs(float x) { return std::fabs(x); }
 inline bool isnan(float x) { return std::isnan(x); }
 inline bool isinf(float x) { return std::isinf(x); }
-/* Needed only so that the unused boundary-integral helpers of the Wendland
- * headers compile; no kernel of the canonical step calls them. */
+/* The analytic Shepard factor of the BI walls (KernelFunctions/Wendland*D.hcl
+ * kernelS_D) */
 inline float sign(float x) { return (x > 0.f) ? 1.f : ((x < 0.f) ? -1.f : 0.f); }
 inline float acospi(float x) { return std::acos(x) / 3.14159265f; }
+inline float atan(float x) { return std::atan(x); }
 
 /* Work-item index: the harness sets it before calling a kernel function */
 extern thread_local usize aqr_gid;
@@ -243,11 +245,15 @@ inline float2 aqr_matrix_dot(const float4& m, const float2& v)
     return float2(m.x * v.x + m.y * v.y, m.z * v.x + m.w * v.y);
 }
 #define MATRIX_DOT(_M, _V) aqr_matrix_dot(_M, _V)
-/* types/2D.h:174-194 -- 9 cells, x offset outermost */
+/* types/2D.h:174-194 -- 9 cells, x offset outermost.  The cell index is
+ * taken modulo 2^32, as the reference computes it where usize is 32 bits:
+ * cfd/Boundary/BI/Interactions.cl passes n_cells as uivec4, so
+ * `__cj * NCELLS.x` is 32-bit unsigned arithmetic, and with a 64-bit usize
+ * the row below (__cj = -1) would land 2^32 cells past the table. */
 #define BEGIN_NEIGHS(CELL, NPARTS, NCELLS, ICELL, IHOC)                        \
     for (int __ci = -1; __ci <= 1; __ci++) {                                   \
         for (int __cj = -1; __cj <= 1; __cj++) {                               \
-            const usize __c_j = CELL + __ci + __cj * NCELLS.x;                 \
+            const usize __c_j = (uint)(CELL + __ci + __cj * NCELLS.x);         \
             usize j = IHOC[__c_j];                                             \
             while ((j < NPARTS) && (ICELL[j] == __c_j)) {
 #define END_NEIGHS()                                                           \

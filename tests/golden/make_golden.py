@@ -16,6 +16,13 @@ GPU host included, can check against them).
   NaN and an out-of-domain particle, random velocities and rates) and the
   Variables after one (out1_*) and two (out2_*) canonical steps of the
   reference-kernel harness.
+* step_bi_{2d,3d}.npz -- the same kind of case with BI walls (cfd/BI.xml in
+  place of cfd/BIe.xml) and the Variables after one, two and five steps
+  (out1_*, out2_*, out5_*) of the harness.
+
+    python tests/golden/make_golden.py [/path/to/reference] [bi]
+
+regenerates everything, or only the BI fixtures with `bi`.
 """
 import os
 import sys
@@ -106,12 +113,38 @@ def make_steps():
         np.savez_compressed(os.path.join(HERE, f"step_{dims}d.npz"), **data)
 
 
+def make_steps_bi():
+    import dataclasses
+    for dims in (2, 3):
+        c = perturbed(small_case(dims), 21 + dims)
+        c.params = dataclasses.replace(c.params, boundary=1)
+        c.u[c.imove == 1] *= 0.25   # gentler flow near the walls
+        st = O.OracleState(c)
+        data = {"in_" + k: getattr(c, k) for k in STATE_KEYS}
+        data.update({"in_t": np.float32(c.t), "in_dt": np.float32(c.dt),
+                     "in_iter": np.uint32(c.iter)})
+        lib = O.load_ref(dims)
+        for step in (1, 2, 3, 4, 5):
+            lib.step(st)
+            if step not in (1, 2, 5):
+                continue
+            for k, a in st.arrays.items():
+                data[f"out{step}_" + k] = (st[k] if k == "ihoc" else a).copy()
+            for k in ("n_cells", "r_min", "r_max", "t", "dt", "iter"):
+                data[f"out{step}_" + k] = np.asarray(st[k])
+        np.savez_compressed(os.path.join(HERE, f"step_bi_{dims}d.npz"), **data)
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     O.build_oracle(ref=True)
+    if len(sys.argv) > 2 and sys.argv[2] == "bi":
+        make_steps_bi()
+        return
     make_linklist(ref_root)
     make_radixsort(ref_root)
     make_steps()
+    make_steps_bi()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
