@@ -76,7 +76,7 @@ class AquaParams(C.Structure):
         ("dr_factor", C.c_float), ("min_bound_dist", C.c_float),
         ("relax_midpoint", C.c_float), ("iter_midpoint_max", C.c_uint32),
         ("refd", _F), ("visc_dyn", _F), ("delta", _F),
-        ("boundary", C.c_int32),
+        ("boundary", C.c_int32), ("scheme", C.c_int32),
     ]
 
 
@@ -207,4 +207,5 @@ def params_struct(p) -> tuple:
     s.iter_midpoint_max = p.iter_midpoint_max
     s.refd, s.visc_dyn, s.delta = (a.ctypes.data_as(_F) for a in keep)
     s.boundary = int(getattr(p, "boundary", 0))
+    s.scheme = int(getattr(p, "scheme", 0))
     return s, keep

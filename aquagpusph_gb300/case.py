@@ -76,6 +76,9 @@ class Params:
     # wall formulation: 0 = BIe (canonical), 1 = BI (analytic Shepard,
     # free-slip boundary integrals)
     boundary: int = 0
+    # time scheme: 0 = midpoint (canonical), 1 = improved Euler
+    # (basic/time_scheme/improved_euler.xml; BI walls only)
+    scheme: int = 0
 
     # compiled Definitions (CalcServer.cpp:235-264, basic.xml:118-129)
     @property

@@ -93,10 +93,19 @@ build_consts(const aqua_params* p, Consts& c)
         p->n_sets > (uint32_t)kMaxSets || !p->refd || !p->visc_dyn ||
         !p->delta || !(p->h > 0.f) || !(p->support > 0.f) || !(p->H > 0.f))
         return AQUA_ERR_INVALID;
-    if (p->iter_midpoint_max != 1)
-        return AQUA_ERR_INVALID;  // one midpoint iteration (canonical stack)
     if (p->boundary != AQUA_BOUNDARY_BIE && p->boundary != AQUA_BOUNDARY_BI)
         return AQUA_ERR_INVALID;
+    if (p->scheme == AQUA_SCHEME_MIDPOINT) {
+        if (p->iter_midpoint_max != 1)
+            return AQUA_ERR_INVALID;  // one midpoint iteration (canonical stack)
+    } else if (p->scheme == AQUA_SCHEME_IMPROVED_EULER) {
+        // BIe/ElasticBounce.cl reads r_in and u_in by sorted index, which
+        // under improved_euler.cl hold the predictor's unsorted output
+        if (p->boundary != AQUA_BOUNDARY_BI)
+            return AQUA_ERR_INVALID;
+    } else {
+        return AQUA_ERR_INVALID;
+    }
     std::memset(&c, 0, sizeof(c));
     c.dims = p->dims;
     c.n_sets = p->n_sets;
@@ -121,6 +130,7 @@ build_consts(const aqua_params* p, Consts& c)
     c.relax_midpoint = p->relax_midpoint;
     c.iter_midpoint_max = p->iter_midpoint_max;
     c.boundary = p->boundary;
+    c.scheme = p->scheme;
     for (uint32_t k = 0; k < p->n_sets; k++) {
         c.refd[k] = p->refd[k];
         c.visc_dyn[k] = p->visc_dyn[k];

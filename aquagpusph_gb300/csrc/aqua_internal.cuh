@@ -41,6 +41,7 @@ struct Consts
     uint32_t iter_midpoint_max;
     float refd[kMaxSets], visc_dyn[kMaxSets], delta[kMaxSets];
     int boundary;       // AQUA_BOUNDARY_BIE or AQUA_BOUNDARY_BI
+    int scheme;         // AQUA_SCHEME_MIDPOINT or AQUA_SCHEME_IMPROVED_EULER
     // derived
     float cell_length;  // support * h (LinkList.cpp:156)
     float idist;        // 1 / (support * h) (LinkList.cl.in:73)

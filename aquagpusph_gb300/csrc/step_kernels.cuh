@@ -20,6 +20,11 @@
 //               midpoint relax + corrector + BIe pst + variable time step
 //               + block min of dt_var (grid minimum by atomicMin)
 //
+// With the improved Euler scheme (basic/time_scheme/improved_euler.xml, BI
+// walls) k_gather runs the improved_euler.cl predictor in place of the
+// midpoint backups, copies and advance, and the sweep epilogue its corrector
+// in place of the midpoint relax and corrector.
+//
 // Every accumulator visits its neighbours in the reference order (27 cells,
 // x offset outermost; particles of a cell in sorted order) and each
 // expression keeps the reference's evaluation order.
@@ -30,6 +35,7 @@
 // warp-wide broadcast.
 //
 // Reference kernels (resources/Scripts/...): basic/time_scheme/midpoint.cl,
+// basic/time_scheme/improved_euler.cl,
 // basic/Domain.cl, basic/Sort.cl, basic/EOS.cl, basic/Binormal.cl,
 // basic/Shepard.cl, cfd/Interactions.cl, cfd/Sensors.cl,
 // cfd/SensorsRenormalization.cl, basic/deltaSPH.cl (lapp, deltaSPH),
@@ -241,10 +247,28 @@ k_gather(Consts c, StepArgs a)
     const float hdt = 0.5f * dt;
     T.cid[s] = kc;
 
-    // Domain (on the predictor backups) + sort stage1
+    const bool heun = c.scheme == AQUA_SCHEME_IMPROVED_EULER;
     int im = S.imove[o];
     float r[4] = { 0.f, 0.f, 0.f, 0.f };
     Vec<D>::load(S.r, o, r);
+    float u0[4] = { 0.f, 0.f, 0.f, 0.f }, ain[4] = { 0.f, 0.f, 0.f, 0.f };
+    Vec<D>::load(S.u, o, u0);
+    Vec<D>::load(S.dudt, o, ain);
+    float rho_in = S.rho[o];
+    const float drhodt_in = S.drhodt[o];
+    if (heun) {
+        // improved_euler.cl predictor: an explicit second-order Taylor step
+        // from the last state (DT = 0 for imove <= 0), before Domain
+        const float DT = (im <= 0) ? 0.f : dt;
+        const float DT2 = 0.5f * DT * DT;
+        for (int k = 0; k < VS; k++) {
+            r[k] = r[k] + DT * u0[k] + DT2 * ain[k];
+            u0[k] = u0[k] + DT * ain[k];
+        }
+        rho_in = rho_in + DT * drhodt_in;
+    }
+
+    // Domain (on the predictor output) + sort stage1
     bool removed = false;
     if (im > -255) {
         bool out = false;
@@ -283,19 +307,18 @@ k_gather(Consts c, StepArgs a)
 
     // sort stage2 (+ Domain zeroing of u_in and m)
     const float m = removed ? 0.f : S.m[o];
-    float uin[4] = { 0.f, 0.f, 0.f, 0.f }, ain[4] = { 0.f, 0.f, 0.f, 0.f };
+    float uin[4] = { 0.f, 0.f, 0.f, 0.f };
     if (!removed)
-        Vec<D>::load(S.u, o, uin);
-    Vec<D>::load(S.dudt, o, ain);
-    const float rho_in = S.rho[o];
-    const float drhodt_in = S.drhodt[o];
+        for (int k = 0; k < 4; k++)
+            uin[k] = u0[k];
 
-    // midpoint advance (imove > 0), midpoint EOS
+    // midpoint advance (imove > 0), midpoint EOS; improved Euler: the EOS of
+    // the sorted predictor output
     float uh[4];
     float rho_h = rho_in;
     for (int k = 0; k < 4; k++)
         uh[k] = uin[k];
-    if (im > 0) {
+    if (!heun && im > 0) {
         for (int k = 0; k < VS; k++)
             uh[k] = uin[k] + hdt * ain[k];
         rho_h = rho_in + hdt * drhodt_in;
@@ -310,12 +333,23 @@ k_gather(Consts c, StepArgs a)
     Vec<D>::store(a.b.r_in, s, r);
     Vec<D>::store(T.u, s, uh);
     Vec<D>::store(a.b.u_in, s, uin);
-    Vec<D>::store(T.dudt, s, ain);
     Vec<D>::store(a.b.dudt_in, s, ain);
+    a.b.drhodt_in[s] = drhodt_in;
+    if (heun) {
+        // Without the midpoint init copies nothing permutes the rates
+        // Variables: until the rates are computed (fluid only, cfd/Rates.cl)
+        // dudt and drhodt keep the last step's order, and BI/GradP.cl reads
+        // a wall's dudt at its new sorted index from them.
+        float a_old[4] = { 0.f, 0.f, 0.f, 0.f };
+        Vec<D>::load(S.dudt, s, a_old);
+        Vec<D>::store(T.dudt, s, a_old);
+        T.drhodt[s] = S.drhodt[s];
+    } else {
+        Vec<D>::store(T.dudt, s, ain);
+        T.drhodt[s] = drhodt_in;
+    }
     T.rho[s] = rho_h;
     a.b.rho_in[s] = rho_in;
-    T.drhodt[s] = drhodt_in;
-    a.b.drhodt_in[s] = drhodt_in;
     T.m[s] = m;
     T.p[s] = p;
     a.b.posq[s] = make_float4(r[0], r[1], D == 3 ? r[2] : 0.f, __int_as_float(im));
@@ -823,25 +857,40 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
             }
         }
     } else {
-        for (int k = 0; k < VS; k++)
-            acc[k] = ain[k];
-        drhodt = drhodt_in;
+        // no rates computed: the Variables keep what k_gather left there
+        // (the sorted old rates under midpoint)
+        Vec<D>::load(T.dudt, i, acc);
+        drhodt = T.drhodt[i];
     }
-    // midpoint relax
-    const float rl = c.relax_midpoint;
-    for (int k = 0; k < VS; k++)
-        acc[k] = rl * ain[k] + (1.f - rl) * acc[k];
-    drhodt = rl * drhodt_in + (1.f - rl) * drhodt;
-    // corrector
     float rin[4] = { 0.f, 0.f, 0.f, 0.f };
     Vec<D>::load(a.b.r_in, i, rin);
-    const float hdt2 = 0.5f * dt * dt;
     float rn_[4] = { 0.f, 0.f, 0.f, 0.f }, un[4] = { 0.f, 0.f, 0.f, 0.f };
-    for (int k = 0; k < VS; k++) {
-        rn_[k] = rin[k] + dt * uin[k] + hdt2 * acc[k];
-        un[k] = uin[k] + dt * acc[k];
+    float rho_n;
+    if (c.scheme == AQUA_SCHEME_IMPROVED_EULER) {
+        // improved_euler.cl corrector: r_in, u_in, rho_in hold the sorted
+        // predictor output
+        const float DT = 0.5f * dt;
+        const float DT2 = DT * DT;
+        for (int k = 0; k < VS; k++) {
+            const float da = acc[k] - ain[k];
+            un[k] = uin[k] + DT * da;
+            rn_[k] = rin[k] + DT2 * da;
+        }
+        rho_n = a.b.rho_in[i] + DT * (drhodt - drhodt_in);
+    } else {
+        // midpoint relax
+        const float rl = c.relax_midpoint;
+        for (int k = 0; k < VS; k++)
+            acc[k] = rl * ain[k] + (1.f - rl) * acc[k];
+        drhodt = rl * drhodt_in + (1.f - rl) * drhodt;
+        // corrector
+        const float hdt2 = 0.5f * dt * dt;
+        for (int k = 0; k < VS; k++) {
+            rn_[k] = rin[k] + dt * uin[k] + hdt2 * acc[k];
+            un[k] = uin[k] + dt * acc[k];
+        }
+        rho_n = a.b.rho_in[i] + dt * drhodt;
     }
-    const float rho_n = a.b.rho_in[i] + dt * drhodt;
     // BIe PST.cl
     if (fluid && bie) {
         const float Ri = 0.5f * powf(T.m[i] / rho_n, 1.f / c.DIMS);
@@ -1039,8 +1088,10 @@ k_bi_walls(Consts c, StepArgs a)
     const uint32_t set_raw = T.iset[i];
     const uint32_t set = set_raw < c.n_sets ? set_raw : 0u;
     const float sh = shep < 1.0e-6f ? 1.f : shep;
+    // the dudt Variable: the sorted old rates (midpoint init copy) or, under
+    // improved Euler, the unpermuted array (see k_gather)
     float dudt[4];
-    Vec<D>::load(a.b.dudt_in, i, dudt);
+    Vec<D>::load(T.dudt, i, dudt);
     float gw[4];
     for (int k = 0; k < VS; k++)
         gw[k] = c.visc_dyn[set] / c.refd[set] * lap[k] / sh + c.g[k] - dudt[k];

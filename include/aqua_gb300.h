@@ -86,10 +86,21 @@ typedef struct
                                   canonical cfd/BIe.xml) or AQUA_BOUNDARY_BI
                                   (cfd/BI.xml: analytic Shepard factor,
                                   free-slip boundary integrals) */
+    int32_t scheme;            /* time scheme: AQUA_SCHEME_MIDPOINT (the
+                                  canonical basic/time_scheme/midpoint.xml,
+                                  iter_midpoint_max = 1) or
+                                  AQUA_SCHEME_IMPROVED_EULER
+                                  (basic/time_scheme/improved_euler.xml;
+                                  BI walls only, as in every reference example
+                                  that uses it -- with BIe walls the elastic
+                                  bounce would read the predictor's unsorted
+                                  r_in/u_in by sorted index) */
 } aqua_params;
 
 #define AQUA_BOUNDARY_BIE 0
 #define AQUA_BOUNDARY_BI 1
+#define AQUA_SCHEME_MIDPOINT 0
+#define AQUA_SCHEME_IMPROVED_EULER 1
 
 /* The particle Variables of one case (all length N; pointers may be host or
  * device memory as each function states).  Fields a call does not use may

@@ -808,8 +808,6 @@ aq_linklist(aq_state* st, const aq_params* pr, int nthreads)
 {
     if (!st || !pr || !st->N)
         return AQ_ERR_INVALID;
-    if (pr->boundary != 0)
-        return AQ_ERR_INVALID;  // BI walls: only the reference-kernel harness
     if (pr->dims == 3) {
         Case<3> cs{ st, pr, threads(nthreads), st->N };
         return linklist<3>(cs);
@@ -825,6 +823,10 @@ extern "C" int
 aq_step(aq_state* st, const aq_params* pr, int nthreads)
 {
     if (!st || !pr || !st->N)
+        return AQ_ERR_INVALID;
+    /* BI walls and the improved Euler scheme: only the reference-kernel
+     * harness */
+    if (pr->boundary != 0 || pr->scheme != 0)
         return AQ_ERR_INVALID;
     if (pr->dims == 3) {
         Case<3> cs{ st, pr, threads(nthreads), st->N };

@@ -58,6 +58,10 @@ typedef struct
     /* wall formulation: 0 = BIe (cfd/BIe.xml, the canonical stack), 1 = BI
      * (cfd/BI.xml: analytic Shepard, free-slip boundary integrals) */
     int32_t boundary;
+    /* time scheme: 0 = midpoint (basic/time_scheme/midpoint.xml), 1 =
+     * improved Euler (basic/time_scheme/improved_euler.xml); only the
+     * reference-kernel harness runs 1 */
+    int32_t scheme;
     /* prescribed roll of the boundary elements and probes (non-fluid
      * particles of set roll_iset) about z through roll_center:
      * psi(t) = roll_amplitude * sin(roll_angular_freq * t), applied after the

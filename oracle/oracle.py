@@ -44,7 +44,7 @@ class AqParams(C.Structure):
         ("dr_factor", C.c_float), ("min_bound_dist", C.c_float),
         ("relax_midpoint", C.c_float), ("iter_midpoint_max", C.c_uint32),
         ("refd", _F), ("visc_dyn", _F), ("delta", _F),
-        ("boundary", C.c_int32),
+        ("boundary", C.c_int32), ("scheme", C.c_int32),
         ("roll_enabled", C.c_int32), ("roll_iset", C.c_uint32),
         ("roll_amplitude", C.c_float), ("roll_angular_freq", C.c_float),
         ("roll_center", C.c_float * 4),
@@ -104,6 +104,7 @@ def make_params(p, motion=None) -> tuple:
     s.iter_midpoint_max = p.iter_midpoint_max
     s.refd, s.visc_dyn, s.delta = (a.ctypes.data_as(_F) for a in keep)
     s.boundary = int(getattr(p, "boundary", 0))
+    s.scheme = int(getattr(p, "scheme", 0))
     if motion is not None:
         s.roll_enabled = 1
         s.roll_iset = motion.iset

@@ -13,7 +13,9 @@
  *   - the preset tool order of one step, basic.xml:132-171 as modified by
  *     basic/time_scheme/midpoint.xml, basic/domain.xml, cfd.xml,
  *     cfd/deltaSPH.xml, cfd/BIe.xml and cfd/variableTimeStep.xml, or with
- *     cfd/BI.xml in place of cfd/BIe.xml (boundary = 1);
+ *     cfd/BI.xml in place of cfd/BIe.xml (boundary = 1), and with
+ *     basic/time_scheme/improved_euler.xml in place of the midpoint scheme
+ *     (scheme = 1);
  *   - the link-list host logic, LinkList.cpp:185-232 (n_cells, float
  *     division by support*h) and LinkList.cpp:326-494 (tool sequence);
  *   - the radix-sort tool as the stable sort it is (RadixSort.cpp:130-304,
@@ -71,6 +73,9 @@ aqr_set_defs(const aq_params* pr)
 
 namespace ref_midpoint {
 #include "resources/Scripts/basic/time_scheme/midpoint.cl"
+}
+namespace ref_improved_euler {
+#include "resources/Scripts/basic/time_scheme/improved_euler.cl"
 }
 namespace ref_domain {
 #include "resources/Scripts/basic/Domain.cl"
@@ -337,11 +342,21 @@ aq_step(aq_state* st, const aq_params* pr, int nthreads)
     std::memcpy(&domain_min, pr->domain_min, sizeof(vec));
     std::memcpy(&domain_max, pr->domain_max, sizeof(vec));
 
-    /* predictor (midpoint.cl:53-75) */
-    ndrange(N, nt, [&]() {
-        ref_midpoint::predictor(r, u, dudt, st->rho, st->drhodt, r_in, u_in,
-                                dudt_in, st->rho_in, st->drhodt_in, N);
-    });
+    const bool ie = pr->scheme == 1;
+    /* predictor (midpoint.cl:53-75 or improved_euler.cl:75-103) */
+    if (ie) {
+        ndrange(N, nt, [&]() {
+            ref_improved_euler::predictor(st->imove, r, u, dudt, st->rho,
+                                          st->drhodt, r_in, u_in, dudt_in,
+                                          st->rho_in, st->drhodt_in, N, dt);
+        });
+    } else {
+        ndrange(N, nt, [&]() {
+            ref_midpoint::predictor(r, u, dudt, st->rho, st->drhodt, r_in,
+                                    u_in, dudt_in, st->rho_in, st->drhodt_in,
+                                    N);
+        });
+    }
     /* Domain (Domain.cl:48-90) */
     ndrange(N, nt, [&]() {
         ref_domain::entry(st->imove, r_in, u_in, dudt_in, st->m, N, domain_min,
@@ -397,24 +412,30 @@ aq_step(aq_state* st, const aq_params* pr, int nthreads)
     std::fill(st->div_u, st->div_u + N, 0.f);
     std::fill(grad_p, grad_p + N, VEC_ZERO);
     std::fill(st->shepard, st->shepard + N, 0.f);
-    /* midpoint init (midpoint.xml) */
-    copy_n(st->drhodt_in, st->drhodt, N);
-    copy_n(dudt_in, dudt, N);
-    copy_n(r, r_in, N);
-    copy_n(u, u_in, N);
-    copy_n(st->rho, st->rho_in, N);
-    for (uint32_t iter_midpoint = 0; iter_midpoint < pr->iter_midpoint_max;
-         iter_midpoint++) {
-        copy_n(st->drhodt, st->drhodt_in, N);
-        copy_n(dudt, dudt_in, N);
-        ndrange(N, nt, [&]() {
-            ref_midpoint::midpoint(st->imove, u_in, u, dudt, st->rho_in,
-                                   st->rho, st->drhodt, N, dt);
-        });
-        ndrange(N, nt, [&]() {
-            ref_eos::entry(st->iset, st->imove, st->rho, st->p, pr->refd, N,
-                           pr->cs, pr->p0);
-        });
+    /* midpoint init (midpoint.xml); the improved Euler scheme has no loop
+     * and none of these tools: the sweeps run once on the sorted predictor
+     * output */
+    if (!ie) {
+        copy_n(st->drhodt_in, st->drhodt, N);
+        copy_n(dudt_in, dudt, N);
+        copy_n(r, r_in, N);
+        copy_n(u, u_in, N);
+        copy_n(st->rho, st->rho_in, N);
+    }
+    const uint32_t passes = ie ? 1u : pr->iter_midpoint_max;
+    for (uint32_t iter_midpoint = 0; iter_midpoint < passes; iter_midpoint++) {
+        if (!ie) {
+            copy_n(st->drhodt, st->drhodt_in, N);
+            copy_n(dudt, dudt_in, N);
+            ndrange(N, nt, [&]() {
+                ref_midpoint::midpoint(st->imove, u_in, u, dudt, st->rho_in,
+                                       st->rho, st->drhodt, N, dt);
+            });
+            ndrange(N, nt, [&]() {
+                ref_eos::entry(st->iset, st->imove, st->rho, st->p, pr->refd,
+                               N, pr->cs, pr->p0);
+            });
+        }
         /* neighbour sweeps; LOCAL_MEM semantics: sums start at zero */
         std::fill(st->shepard, st->shepard + N, 0.f);
         if (bi) {
@@ -509,16 +530,26 @@ aq_step(aq_state* st, const aq_params* pr, int nthreads)
                                           dudt, N, dt, icell, ihoc, n_cells);
             });
         }
+        if (!ie) {
+            ndrange(N, nt, [&]() {
+                ref_midpoint::relax(st->imove, dudt_in, dudt, st->drhodt_in,
+                                    st->drhodt, N, pr->relax_midpoint);
+            });
+        }
+    }
+    /* corrector (midpoint.cl:206-227 or improved_euler.cl:125-147), PST */
+    if (ie) {
         ndrange(N, nt, [&]() {
-            ref_midpoint::relax(st->imove, dudt_in, dudt, st->drhodt_in,
-                                st->drhodt, N, pr->relax_midpoint);
+            ref_improved_euler::corrector(st->imove, st->iset, r, u, dudt,
+                                          st->rho, st->drhodt, dudt_in,
+                                          st->drhodt_in, N, dt);
+        });
+    } else {
+        ndrange(N, nt, [&]() {
+            ref_midpoint::corrector(st->imove, r_in, r, u_in, u, dudt,
+                                    st->rho_in, st->rho, st->drhodt, N, dt);
         });
     }
-    /* corrector, PST */
-    ndrange(N, nt, [&]() {
-        ref_midpoint::corrector(st->imove, r_in, r, u_in, u, dudt, st->rho_in,
-                                st->rho, st->drhodt, N, dt);
-    });
     if (!bi) {
         ndrange(N, nt, [&]() {
             ref_pst::entry(st->imove, r, normal, st->m, st->rho, N, icell,

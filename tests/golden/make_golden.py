@@ -19,10 +19,13 @@ GPU host included, can check against them).
 * step_bi_{2d,3d}.npz -- the same kind of case with BI walls (cfd/BI.xml in
   place of cfd/BIe.xml) and the Variables after one, two and five steps
   (out1_*, out2_*, out5_*) of the harness.
+* step_ie_{2d,3d}.npz -- BI walls with the improved Euler scheme
+  (basic/time_scheme/improved_euler.xml in place of the midpoint scheme, as
+  in the reference's BI examples), after one, two and five steps.
 
-    python tests/golden/make_golden.py [/path/to/reference] [bi]
+    python tests/golden/make_golden.py [/path/to/reference] [bi|ie]
 
-regenerates everything, or only the BI fixtures with `bi`.
+regenerates everything, or only the BI or improved-Euler fixtures.
 """
 import os
 import sys
@@ -113,11 +116,11 @@ def make_steps():
         np.savez_compressed(os.path.join(HERE, f"step_{dims}d.npz"), **data)
 
 
-def make_steps_bi():
+def make_steps_bi(scheme=0):
     import dataclasses
     for dims in (2, 3):
-        c = perturbed(small_case(dims), 21 + dims)
-        c.params = dataclasses.replace(c.params, boundary=1)
+        c = perturbed(small_case(dims), (31 if scheme else 21) + dims)
+        c.params = dataclasses.replace(c.params, boundary=1, scheme=scheme)
         c.u[c.imove == 1] *= 0.25   # gentler flow near the walls
         st = O.OracleState(c)
         data = {"in_" + k: getattr(c, k) for k in STATE_KEYS}
@@ -132,19 +135,21 @@ def make_steps_bi():
                 data[f"out{step}_" + k] = (st[k] if k == "ihoc" else a).copy()
             for k in ("n_cells", "r_min", "r_max", "t", "dt", "iter"):
                 data[f"out{step}_" + k] = np.asarray(st[k])
-        np.savez_compressed(os.path.join(HERE, f"step_bi_{dims}d.npz"), **data)
+        name = "step_ie" if scheme else "step_bi"
+        np.savez_compressed(os.path.join(HERE, f"{name}_{dims}d.npz"), **data)
 
 
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     O.build_oracle(ref=True)
-    if len(sys.argv) > 2 and sys.argv[2] == "bi":
-        make_steps_bi()
+    if len(sys.argv) > 2 and sys.argv[2] in ("bi", "ie"):
+        make_steps_bi(1 if sys.argv[2] == "ie" else 0)
         return
     make_linklist(ref_root)
     make_radixsort(ref_root)
     make_steps()
     make_steps_bi()
+    make_steps_bi(scheme=1)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -1,6 +1,8 @@
 """BI walls (cfd/BI.xml in place of cfd/BIe.xml) on the GPU against the
 golden fixtures that the reference's own BI kernels produced through the
-reference-kernel harness (tests/golden/step_bi_{2d,3d}.npz).
+reference-kernel harness: with the midpoint scheme
+(tests/golden/step_bi_{2d,3d}.npz) and with the improved Euler scheme
+(basic/time_scheme/improved_euler.xml, tests/golden/step_ie_{2d,3d}.npz).
 
 The analytic Shepard factor goes through atan (2-D) and acos (3-D), whose
 last bits differ between CUDA and the host libm, so after the link-list
@@ -31,11 +33,15 @@ def gpu():
     return torch
 
 
-def fixture_case(dims):
+SCHEMES = {"bi": 0, "ie": 1}
+
+
+def fixture_case(dims, name="bi"):
     from golden_cases import small_case
-    d = np.load(os.path.join(GOLD, f"step_bi_{dims}d.npz"))
+    d = np.load(os.path.join(GOLD, f"step_{name}_{dims}d.npz"))
     base = small_case(dims)
-    c = cases.Case(dataclasses.replace(base.params, boundary=1),
+    c = cases.Case(dataclasses.replace(base.params, boundary=1,
+                                       scheme=SCHEMES[name]),
                    len(d["in_r"]))
     for k in STATE:
         getattr(c, k)[...] = d["in_" + k]
@@ -55,15 +61,17 @@ def close(a, b, mask=None):
     return float(np.abs(a[fin] - b[fin]).max() / max(np.abs(b[fin]).max(), 1e-30))
 
 
+@pytest.mark.parametrize("name", ["bi", "ie"])
 @pytest.mark.parametrize("dims", [2, 3])
-def test_bi_one_step_matches_reference_kernels(gpu, dims):
+def test_bi_one_step_matches_reference_kernels(gpu, dims, name):
     from aquagpusph_gb300.solver import Solver
-    c, d = fixture_case(dims)
+    c, d = fixture_case(dims, name)
     sv = Solver(c.params, capacity=c.N)
     sv.set_extras(True)
     sv.set_case(c)
     assert sv.launches_per_step() == 1 + Solver(  # one launch more than BIe
-        dataclasses.replace(c.params, boundary=0), capacity=c.N).launches_per_step()
+        dataclasses.replace(c.params, boundary=0, scheme=0),
+        capacity=c.N).launches_per_step()
     sv.step(1, graph=False)
     sv.check()
     g = sv.get_case()
@@ -85,13 +93,20 @@ def test_bi_one_step_matches_reference_kernels(gpu, dims):
     active = (d["out1_imove"] >= -3) & (d["out1_imove"] <= 1)
     errs["shepard"] = close(sh[active], d["out1_shepard"][active])
     assert max(errs.values()) <= 1e-5, errs
+    if name == "ie":
+        # the rates Variables of every particle whose rates are not computed
+        # are the unpermuted old arrays, copied bit for bit
+        nf = ~fl
+        assert np.array_equal(g.dudt[nf], d["out1_dudt"][nf])
+        assert np.array_equal(g.drhodt[nf], d["out1_drhodt"][nf])
     sv.close()
 
 
+@pytest.mark.parametrize("name", ["bi", "ie"])
 @pytest.mark.parametrize("dims", [2, 3])
-def test_bi_five_steps_match_reference_kernels(gpu, dims):
+def test_bi_five_steps_match_reference_kernels(gpu, dims, name):
     from aquagpusph_gb300.solver import Solver
-    c, d = fixture_case(dims)
+    c, d = fixture_case(dims, name)
     sv = Solver(c.params, capacity=c.N)
     sv.set_case(c)
     sv.step(5, graph=True)
@@ -106,10 +121,11 @@ def test_bi_five_steps_match_reference_kernels(gpu, dims):
     sv.close()
 
 
-def test_bi_fast_build_close_to_exact(gpu):
+@pytest.mark.parametrize("name", ["bi", "ie"])
+def test_bi_fast_build_close_to_exact(gpu, name):
     """The fast build stays within 1e-4 of the exact one over three steps."""
     from aquagpusph_gb300.solver import Solver
-    c, d = fixture_case(2)
+    c, d = fixture_case(2, name)
     runs = []
     for fast in (False, True):
         sv = Solver(c.params, capacity=c.N)
@@ -124,3 +140,12 @@ def test_bi_fast_build_close_to_exact(gpu):
     ia, ib = np.argsort(a.id), np.argsort(b.id)
     for k in ("r", "u", "rho"):
         assert close(getattr(b, k)[ib], getattr(a, k)[ia]) <= 1e-4, k
+
+
+def test_improved_euler_needs_bi_walls(gpu):
+    """BIe walls with the improved Euler scheme are refused at creation."""
+    from aquagpusph_gb300 import _lib
+    from aquagpusph_gb300.solver import Solver
+    c, _ = fixture_case(2, "ie")
+    with pytest.raises(_lib.AquaError):
+        Solver(dataclasses.replace(c.params, boundary=0), capacity=c.N)
