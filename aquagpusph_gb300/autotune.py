@@ -19,11 +19,14 @@ from . import _lib
 
 # (variant, threads per block, queued neighbours per thread); the variant
 # numbers are those of aqua_set_tuning (3 and 4 stage the candidates with
-# bulk copies)
+# bulk copies, 5 and 6 sum each candidate group directly, without a queue,
+# 7 and 8 too, with the next group prefetched by asynchronous copies, 9-12
+# those compiled for 28 or 32 resident warps per SM)
 VARIANTS = ((0, 128, 128), (1, 64, 128), (2, 64, 64), (3, 64, 128),
-            (4, 64, 64))
+            (4, 64, 64), (5, 64, 0), (6, 128, 0), (7, 64, 0), (8, 128, 0),
+            (9, 64, 0), (10, 128, 0), (11, 64, 0), (12, 128, 0))
 # resident warps per SM tried for each variant (blocks = warps * 32 / threads)
-WARPS_PER_SM = (8, 10, 12, 16, 20, 24)
+WARPS_PER_SM = (8, 10, 12, 16, 20, 24, 28, 32)
 MAX_BLOCKS_PER_SM = 32
 
 

@@ -11,12 +11,17 @@ constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
 // sweep variants: threads per block x queued neighbours per thread (the
 // staging depth) x queue entry x candidate staging: 0 = (128, 128, 16-bit,
 // loads), 1 = (64, 128, 16-bit, loads), 2 = (64, 64, 32-bit, loads),
-// 3 = (64, 128, 16-bit, bulk copies), 4 = (64, 64, 32-bit, bulk copies)
-constexpr int kSweepVariants = 5;
+// 3 = (64, 128, 16-bit, bulk copies), 4 = (64, 64, 32-bit, bulk copies);
+// direct sweep (no queue, each candidate group summed as it is loaded):
+// 5 = 64 threads, 6 = 128 threads, and with the next group's records
+// prefetched by asynchronous copies: 7 = 64 threads, 8 = 128 threads;
+// those with the register budget of 28 resident warps per SM (9 = 64,
+// 10 = 128 threads) or 32 (11 = 64, 12 = 128 threads)
+constexpr int kSweepVariants = 13;
 inline int
 sweep_variant_threads(int v)
 {
-    return v == 0 ? 128 : 64;
+    return (v == 0 || v == 6 || v == 8 || v == 10 || v == 12) ? 128 : 64;
 }
 
 // The reference's vec type: float4 in 3-D, float2 in 2-D

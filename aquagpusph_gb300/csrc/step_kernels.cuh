@@ -49,6 +49,40 @@ namespace {
 
 constexpr uint32_t kBulkWaitLimit = 1u << 20;  // bounded mbarrier polls
 
+// How the sweep hands in-support candidates to the pair arithmetic: per-lane
+// ring queues drained with full warps, or directly, each survivor of a group
+// summed at once by the lanes it reaches
+constexpr int kSweepQueue = 0;
+constexpr int kSweepDirect = 1;
+
+// Ampere-style asynchronous copies global -> shared (no registers held while
+// in flight), grouped and waited for per thread
+__device__ __forceinline__ void
+cp_async_16(void* smem, const void* gmem)
+{
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n"
+                 :: "r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void
+cp_async_8(void* smem, const void* gmem)
+{
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n"
+                 :: "r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void
+cp_async_commit()
+{
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// waits until at most one committed group of this thread is in flight
+__device__ __forceinline__ void
+cp_async_wait_all_but_one()
+{
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+}
+
 // Wendland C2 (Wendland{2D,3D}.hcl:44-66); the constants are float
 // products folded at compile time, as the OpenCL compiler folds them
 template<int D>
@@ -378,11 +412,11 @@ k_gather(Consts c, StepArgs a)
 // neighbour cells of the warp's cell.  The scan checks the queues every 32
 // candidates, where they have room for at least 32 more, so a queue never
 // overflows.
-template<int D, int NT, int NQ, typename QE, bool BULK, bool BI>
+template<int D, int NT, int NQ, typename QE, bool BULK, bool BI, int MODE>
 __device__ __forceinline__ float
 sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                QE* queue, uint32_t* cstart, float4* grp2, uint64_t* mbar,
-               uint32_t& phases)
+               uint32_t& phases, float4* vel_s, float2* pm_s)
 {
     constexpr int VS = Vec<D>::VS;
     constexpr int NC = (D == 3) ? 27 : 9;
@@ -416,6 +450,65 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     const float ri[3] = { pi.x, pi.y, pi.z };
     const float uiv[3] = { vi.x, vi.y, vi.z };
 
+    // One neighbour j of the sums (its packed records pj, vj, pmj), taken in
+    // visiting order; the support test is the reference's q >= SUPPORT.
+    auto pair = [&](uint32_t j, const float4 pj, const float4 vj,
+                    const float2 pmj) {
+        const int jm = __float_as_int(pj.w);
+        float d[3];
+        d[0] = pj.x - ri[0];
+        d[1] = pj.y - ri[1];
+        d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
+        const float rr = dot_d<D>(d, d);
+        const float q = sqrtf(rr) / c.H;
+        if (q >= c.SUPPORT)
+            return;
+        if (jm == 1) {
+            const float rho_j = vj.w, m_j = pmj.y;
+            const float wj = kernel_w<D>(q) * c.CONW * m_j / rho_j;
+            shep = shep + wj;
+            if (j == i)
+                return;
+            if (fluid) {
+                const float p_j = pmj.x;
+                float dv[3];
+                dv[0] = vj.x - uiv[0];
+                dv[1] = vj.y - uiv[1];
+                dv[2] = (D == 3) ? vj.z - uiv[2] : 0.f;
+                const float udr = dot_d<D>(dv, d);
+                const float f_ij = kernel_f<D>(q) * c.CONF * m_j;
+                const float rr_ij = rho_i * rho_j;
+                const float sgp = (p_i + p_j) / rr_ij * f_ij;
+                const float slu = f_ij * 2.f / rr_ij;
+                for (int kk = 0; kk < D; kk++) {
+                    gp[kk] = gp[kk] + sgp * d[kk];
+                    lu[kk] = lu[kk] + slu * dv[kk];
+                }
+                du = du + udr * f_ij * rho_i / rho_j;
+                lp = lp + (p_j - p_i) * (f_ij / rho_j);
+            } else if (sensor) {
+                su[0] = su[0] + vj.x * wj;
+                su[1] = su[1] + vj.y * wj;
+                if (D == 3)
+                    su[2] = su[2] + vj.z * wj;
+                sr = sr + rho_j * wj;
+                sp = sp + pmj.x * wj;
+            }
+        } else {
+            // boundary element: BIe wall sums (fluid i only)
+            float nj[3];
+            load_normal<D>(a.dst.normal, j, nj);
+            const float uj[3] = { vj.x, vj.y, vj.z };
+            const float wa = kernel_w<D>(q) * c.CONW * pmj.y;
+            float g[3];
+            for (int kk = 0; kk < D; kk++) {
+                g[kk] = nj[kk] * wa;
+                gw[kk] = gw[kk] + g[kk];
+            }
+            dbi = dbi - dot_d<D>(uj, g);
+        }
+    };
+
     uint32_t qh = 0, qt = 0;  // ring queue head / tail
     // The drain is software-pipelined: the records of the next queued
     // neighbour are loaded while the current pair is computed.
@@ -443,59 +536,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
             const float2 pmj = mn;
             if (qh + 1 < upto)
                 fetch(qh + 1);
-            const int jm = __float_as_int(pj.w);
-            float d[3];
-            d[0] = pj.x - ri[0];
-            d[1] = pj.y - ri[1];
-            d[2] = (D == 3) ? pj.z - ri[2] : 0.f;
-            const float rr = dot_d<D>(d, d);
-            const float q = sqrtf(rr) / c.H;
-            if (q >= c.SUPPORT)
-                continue;
-            if (jm == 1) {
-                    const float rho_j = vj.w, m_j = pmj.y;
-                    const float wj = kernel_w<D>(q) * c.CONW * m_j / rho_j;
-                    shep = shep + wj;
-                    if (j == i)
-                        continue;
-                    if (fluid) {
-                        const float p_j = pmj.x;
-                        float dv[3];
-                        dv[0] = vj.x - uiv[0];
-                        dv[1] = vj.y - uiv[1];
-                        dv[2] = (D == 3) ? vj.z - uiv[2] : 0.f;
-                        const float udr = dot_d<D>(dv, d);
-                        const float f_ij = kernel_f<D>(q) * c.CONF * m_j;
-                        const float rr_ij = rho_i * rho_j;
-                        const float sgp = (p_i + p_j) / rr_ij * f_ij;
-                        const float slu = f_ij * 2.f / rr_ij;
-                        for (int kk = 0; kk < D; kk++) {
-                            gp[kk] = gp[kk] + sgp * d[kk];
-                            lu[kk] = lu[kk] + slu * dv[kk];
-                        }
-                        du = du + udr * f_ij * rho_i / rho_j;
-                        lp = lp + (p_j - p_i) * (f_ij / rho_j);
-                    } else if (sensor) {
-                        su[0] = su[0] + vj.x * wj;
-                        su[1] = su[1] + vj.y * wj;
-                        if (D == 3)
-                            su[2] = su[2] + vj.z * wj;
-                        sr = sr + rho_j * wj;
-                        sp = sp + pmj.x * wj;
-                    }
-                } else {
-                    // boundary element: BIe wall sums (fluid i only)
-                    float nj[3];
-                    load_normal<D>(a.dst.normal, j, nj);
-                    const float uj[3] = { vj.x, vj.y, vj.z };
-                    const float wa = kernel_w<D>(q) * c.CONW * pmj.y;
-                    float g[3];
-                    for (int kk = 0; kk < D; kk++) {
-                        g[kk] = nj[kk] * wa;
-                        gw[kk] = gw[kk] + g[kk];
-                    }
-                    dbi = dbi - dot_d<D>(uj, g);
-                }
+            pair(j, pj, vj, pmj);
         }
     };
 
@@ -544,7 +585,16 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         return true;
     };
     auto issue = [&](int b, const uint2 se, uint32_t g) {
-        if (BULK && lane == 0) {
+        if constexpr (BULK && MODE == kSweepDirect) {
+            // every lane copies its candidate's three records; committed by
+            // the caller as one group per candidate group
+            const uint32_t j = se.x + g + lane;
+            if (g + lane < se.y - se.x) {
+                cp_async_16(grp2 + 32 * b + lane, a.b.posq + j);
+                cp_async_16(vel_s + 32 * b + lane, a.b.velq + j);
+                cp_async_8(pm_s + 32 * b + lane, a.b.pmq + j);
+            }
+        } else if (BULK && lane == 0) {
             const uint32_t bytes = min(32u, se.y - se.x - g) * 16u;
             const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[b]);
             const uint32_t dst = (uint32_t)__cvta_generic_to_shared(grp2 + 32 * b);
@@ -559,6 +609,12 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         }
     };
     auto wait = [&](int b) -> bool {
+        if constexpr (MODE == kSweepDirect) {
+            // the group before the newest is this one
+            cp_async_wait_all_but_one();
+            __syncwarp();
+            return true;
+        }
         const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[b]);
         const uint32_t par = (phases >> b) & 1u;
         uint32_t done = 0;
@@ -578,6 +634,8 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     int buf = 0;
     if (BULK && have)
         issue(0, se, g);
+    if (BULK && MODE == kSweepDirect)
+        cp_async_commit();
     while (have) {
         int kn = k;
         uint2 sen = se;
@@ -585,14 +643,17 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         const bool hn = advance(kn, sen, gn);
         if (BULK && hn)
             issue(buf ^ 1, sen, gn);
+        if (BULK && MODE == kSweepDirect)
+            cp_async_commit();  // possibly empty: one group per iteration
         // warp-uniform checkpoint: make room for the next 32 candidates,
         // first draining the entries every lane has (full warps)
-        if (__any_sync(0xffffffffu, qt - qh > NQ - 32)) {
+        constexpr uint32_t room = NQ > 32 ? (uint32_t)(NQ - 32) : 0u;
+        if (MODE == kSweepQueue && __any_sync(0xffffffffu, qt - qh > room)) {
             const uint32_t fill = qt - qh;
             const uint32_t common = __reduce_min_sync(
                 0xffffffffu, want_shep ? fill : 0xffffffffu);
             drain(qh + min(common, fill));
-            if (__any_sync(0xffffffffu, qt - qh > NQ - 32))
+            if (__any_sync(0xffffffffu, qt - qh > room))
                 drain(qt);
         }
         const uint32_t count = se.y - se.x;
@@ -629,6 +690,35 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
             cand = (jm == 1 || jm == -3) && bb < q2_box;
         }
         uint32_t bal = __ballot_sync(0xffffffffu, cand);
+        if constexpr (MODE == kSweepDirect) {
+            // the survivors' other records (prefetched with the group, or
+            // one coalesced load per lane); then every survivor, in visiting
+            // order, is summed at once by the lanes whose particle it reaches
+            float4* vel = vel_s + (BULK ? 32 * buf : 0);
+            float2* pm = pm_s + (BULK ? 32 * buf : 0);
+            if constexpr (!BULK) {
+                if (cand) {
+                    vel[lane] = a.b.velq[se.x + g + lane];
+                    pm[lane] = a.b.pmq[se.x + g + lane];
+                }
+                __syncwarp();
+            }
+            while (bal) {
+                const uint32_t b = __ffs(bal) - 1;
+                bal &= bal - 1;
+                const float4 pj = grp[b];
+                const int jm = __float_as_int(pj.w);
+                const float d0 = pj.x - ri[0], d1 = pj.y - ri[1];
+                float rr = d0 * d0 + d1 * d1;
+                if (D == 3) {
+                    const float d2 = pj.z - ri[2];
+                    rr = rr + d2 * d2;
+                }
+                if (want_shep && (jm == 1 || (bie && fluid && jm == -3)) &&
+                    rr < c.q2_reject)
+                    pair(se.x + g + b, pj, vel[b], pm[b]);
+            }
+        }
         auto consider = [&](const float4 pj, uint32_t off) {
             const int jm = __float_as_int(pj.w);
             const float d0 = pj.x - ri[0], d1 = pj.y - ri[1];
@@ -648,7 +738,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                 qt++;
             }
         };
-        while (bal) {
+        while (MODE == kSweepQueue && bal) {
             // two survivors per iteration, in visiting order
             const uint32_t b0 = __ffs(bal) - 1;
             bal &= bal - 1;
@@ -669,7 +759,8 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         have = hn;
         buf ^= 1;
     }
-    drain(qt);
+    if constexpr (MODE == kSweepQueue)
+        drain(qt);
     if (!valid)
         return INFINITY;
     if constexpr (BI) {
@@ -939,11 +1030,18 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
 // NT threads per block, NQ queued neighbours per thread (power of 2, >= 64)
 // of type QE, candidate groups copied by the bulk-copy engine when BULK,
 // BI walls (cfd/BI.xml) when BI, else BIe walls
-template<int D, int NT, int NQ, typename QE, bool BULK, bool BI>
-__global__ void __launch_bounds__(NT, 640 / NT)
+template<int D, int NT, int NQ, typename QE, bool BULK, bool BI, int MODE,
+         int MINW = 20>
+__global__ void __launch_bounds__(NT, MINW * 32 / NT)
 k_sweep(Consts c, StepArgs a)
 {
-    __shared__ QE s_queue[NQ * NT];
+    // per-lane queues, or (direct) per warp the velocity/density and
+    // pressure/mass records of the current candidate group (two buffers each
+    // when the groups are prefetched)
+    constexpr int WP = (MODE == kSweepQueue) ? 1 : NT / 32;
+    __shared__ QE s_queue[MODE == kSweepQueue ? NQ * NT : 1];
+    __shared__ __align__(16) float4 s_vel[WP][2 * 32];
+    __shared__ __align__(8) float2 s_pm[WP][2 * 32];
     __shared__ uint32_t s_cstart[NT / 32][32];
     __shared__ __align__(16) float4 s_grp[NT / 32][2 * 32];
     __shared__ __align__(8) uint64_t s_mbar[NT / 32][2];
@@ -978,9 +1076,11 @@ k_sweep(Consts c, StepArgs a)
                 break;
             const uint2 cw = a.b.chunks[ch];
             const bool valid = (uint32_t)lane < cw.y;
-            float v = sweep_particle<D, NT, NQ, QE, BULK, BI>(
-                c, a, valid ? cw.x + lane : cw.x, valid, s_queue + threadIdx.x,
-                s_cstart[warp], s_grp[warp], s_mbar[warp], phases);
+            float v = sweep_particle<D, NT, NQ, QE, BULK, BI, MODE>(
+                c, a, valid ? cw.x + lane : cw.x, valid,
+                s_queue + (MODE == kSweepQueue ? threadIdx.x : 0),
+                s_cstart[warp], s_grp[warp], s_mbar[warp], phases,
+                s_vel[WP > 1 ? warp : 0], s_pm[WP > 1 ? warp : 0]);
             __syncwarp();  // s_cstart and s_grp are rewritten for the next chunk
             for (int o = 16; o > 0; o >>= 1)
                 v = cl_min(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -1154,8 +1254,8 @@ launch_gather_impl(const Consts& c, const StepArgs& a, cudaStream_t s)
 }
 
 // sweep variants the tuner chooses from: (threads per block, queue depth,
-// queue entry type, bulk-copy staging); a block's static shared memory
-// stays <= 37 KB
+// queue entry type, bulk-copy staging) for the queued sweep, or threads per
+// block for the direct one; a block's static shared memory stays <= 37 KB
 template<int D>
 cudaError_t
 launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
@@ -1165,24 +1265,49 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
         return cudaSuccess;
     if (c.boundary == AQUA_BOUNDARY_BI) {
         // one launch shape for the BI walls
-        k_sweep<D, 64, 128, uint16_t, false, true><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 128, uint16_t, false, true, kSweepQueue><<<grid, 64, 0, s>>>(c, a);
         return cudaGetLastError();
     }
     switch (variant) {
     case 1:
-        k_sweep<D, 64, 128, uint16_t, false, false><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 128, uint16_t, false, false, kSweepQueue><<<grid, 64, 0, s>>>(c, a);
         break;
     case 2:
-        k_sweep<D, 64, 64, uint32_t, false, false><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 64, uint32_t, false, false, kSweepQueue><<<grid, 64, 0, s>>>(c, a);
         break;
     case 3:
-        k_sweep<D, 64, 128, uint16_t, true, false><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 128, uint16_t, true, false, kSweepQueue><<<grid, 64, 0, s>>>(c, a);
         break;
     case 4:
-        k_sweep<D, 64, 64, uint32_t, true, false><<<grid, 64, 0, s>>>(c, a);
+        k_sweep<D, 64, 64, uint32_t, true, false, kSweepQueue><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 5:
+        k_sweep<D, 64, 1, uint32_t, false, false, kSweepDirect><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 6:
+        k_sweep<D, 128, 1, uint32_t, false, false, kSweepDirect><<<grid, 128, 0, s>>>(c, a);
+        break;
+    case 7:
+        k_sweep<D, 64, 1, uint32_t, true, false, kSweepDirect><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 8:
+        k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect><<<grid, 128, 0, s>>>(c, a);
+        break;
+    // the same with the register budget of 28 or 32 resident warps per SM
+    case 9:
+        k_sweep<D, 64, 1, uint32_t, true, false, kSweepDirect, 28><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 10:
+        k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect, 28><<<grid, 128, 0, s>>>(c, a);
+        break;
+    case 11:
+        k_sweep<D, 64, 1, uint32_t, true, false, kSweepDirect, 32><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 12:
+        k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect, 32><<<grid, 128, 0, s>>>(c, a);
         break;
     default:
-        k_sweep<D, 128, 128, uint16_t, false, false><<<grid, 128, 0, s>>>(c, a);
+        k_sweep<D, 128, 128, uint16_t, false, false, kSweepQueue><<<grid, 128, 0, s>>>(c, a);
         break;
     }
     return cudaGetLastError();

@@ -212,8 +212,12 @@ aqua_status aqua_set_precision(aqua_ctx* ctx, int mode);
  * queued neighbours per thread, the queue entry and how candidate groups
  * reach shared memory (0: 128 x 128 16-bit loads, 1: 64 x 128 16-bit loads,
  * 2: 64 x 64 32-bit loads, 3: 64 x 128 16-bit bulk copies, 4: 64 x 64
- * 32-bit bulk copies), `blocks_per_sm` the persistent grid (blocks per SM,
- * <= 32).
+ * 32-bit bulk copies), or the direct sweep that sums each candidate group
+ * as it is loaded, without a queue (5: 64 threads, 6: 128 threads; 7: 64
+ * and 8: 128 threads with the next group prefetched by asynchronous
+ * copies; 9: 64 and 10: 128 threads of those compiled for 28 resident warps
+ * per SM, 11: 64 and 12: 128 threads for 32);
+ * `blocks_per_sm` the persistent grid (blocks per SM, <= 32).
  * Any choice gives the same results; aquagpusph_gb300.autotune picks the
  * fastest for a case by timing them. */
 aqua_status aqua_set_tuning(aqua_ctx* ctx, uint32_t sweep_variant,

@@ -1,7 +1,7 @@
-"""Launch shapes of the sweep (threads per block, queue depth, persistent
-blocks per SM) change only the schedule: each particle's neighbours are
-still summed in the link-list order, so every shape gives bit-identical
-state with the exact build.  The tuner picks one of them and the solver
+"""Launch shapes of the sweep (threads per block, queue depth, the direct
+sweep without a queue, persistent blocks per SM) change only the schedule:
+each particle's neighbours are still summed in the link-list order, so every
+shape gives bit-identical state, with the exact and with the fast build.  The tuner picks one of them and the solver
 keeps stepping correctly."""
 import numpy as np
 import pytest
@@ -42,7 +42,9 @@ def run(c, variant, blocks, steps=3, fast=False):
     return g
 
 
-SHAPES = [(0, 2), (0, 5), (1, 10), (2, 4), (3, 8), (4, 12)]
+SHAPES = [(0, 2), (0, 5), (1, 10), (2, 4), (3, 8), (4, 12), (5, 10), (5, 3),
+          (6, 6), (7, 12), (7, 2), (8, 6), (9, 14), (10, 7), (11, 16),
+          (12, 8)]
 
 
 @pytest.mark.parametrize("fast", [False, True])
