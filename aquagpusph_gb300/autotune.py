@@ -17,16 +17,19 @@ import time
 
 from . import _lib
 
-# (variant, threads per block, queued neighbours per thread); the variant
-# numbers are those of aqua_set_tuning (3 and 4 stage the candidates with
-# bulk copies, 5 and 6 sum each candidate group directly, without a queue,
-# 7 and 8 too, with the next group prefetched by asynchronous copies, 9-12
-# those compiled for 28 or 32 resident warps per SM)
-VARIANTS = ((0, 128, 128), (1, 64, 128), (2, 64, 64), (3, 64, 128),
-            (4, 64, 64), (5, 64, 0), (6, 128, 0), (7, 64, 0), (8, 128, 0),
-            (9, 64, 0), (10, 128, 0), (11, 64, 0), (12, 128, 0))
+# (variant, threads per block, queued neighbours per thread, the most
+# resident warps per SM its register budget allows); the variant numbers are
+# those of aqua_set_tuning (3 and 4 stage the candidates with bulk copies,
+# 5 and 6 sum each candidate group directly, without a queue, 7 and 8 too,
+# with the next group prefetched by asynchronous copies, 9-16 those
+# compiled for 28, 32, 36 or 40 resident warps per SM)
+VARIANTS = ((0, 128, 128, 24), (1, 64, 128, 24), (2, 64, 64, 24),
+            (3, 64, 128, 24), (4, 64, 64, 24), (5, 64, 0, 24), (6, 128, 0, 24),
+            (7, 64, 0, 24), (8, 128, 0, 24), (9, 64, 0, 28), (10, 128, 0, 28),
+            (11, 64, 0, 32), (12, 128, 0, 32), (13, 64, 0, 36),
+            (14, 128, 0, 36), (15, 64, 0, 40), (16, 128, 0, 40))
 # resident warps per SM tried for each variant (blocks = warps * 32 / threads)
-WARPS_PER_SM = (8, 10, 12, 16, 20, 24, 28, 32)
+WARPS_PER_SM = (8, 12, 16, 20, 24, 28, 32, 36, 40)
 MAX_BLOCKS_PER_SM = 32
 
 
@@ -79,8 +82,10 @@ def _save(d):
 
 
 def candidates():
-    for v, threads, queue in VARIANTS:
+    for v, threads, queue, most in VARIANTS:
         for w in WARPS_PER_SM:
+            if w > most:
+                continue
             b = w * 32 // threads
             if b * threads == w * 32 and 1 <= b <= MAX_BLOCKS_PER_SM:
                 yield v, b

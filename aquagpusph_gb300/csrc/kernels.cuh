@@ -16,12 +16,12 @@ constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
 // 5 = 64 threads, 6 = 128 threads, and with the next group's records
 // prefetched by asynchronous copies: 7 = 64 threads, 8 = 128 threads;
 // those with the register budget of 28 resident warps per SM (9 = 64,
-// 10 = 128 threads) or 32 (11 = 64, 12 = 128 threads)
-constexpr int kSweepVariants = 13;
+// 10 = 128 threads), 32 (11, 12), 36 (13, 14) or 40 (15, 16)
+constexpr int kSweepVariants = 17;
 inline int
 sweep_variant_threads(int v)
 {
-    return (v == 0 || v == 6 || v == 8 || v == 10 || v == 12) ? 128 : 64;
+    return (v == 0 || (v >= 6 && v % 2 == 0)) ? 128 : 64;
 }
 
 // The reference's vec type: float4 in 3-D, float2 in 2-D

@@ -416,7 +416,7 @@ template<int D, int NT, int NQ, typename QE, bool BULK, bool BI, int MODE>
 __device__ __forceinline__ float
 sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                QE* queue, uint32_t* cstart, float4* grp2, uint64_t* mbar,
-               uint32_t& phases, float4* vel_s, float2* pm_s)
+               uint32_t& phases, float4* vel_s, float2* pm_s, float* box_s)
 {
     constexpr int VS = Vec<D>::VS;
     constexpr int NC = (D == 3) ? 27 : 9;
@@ -441,9 +441,8 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     float gp[3] = { 0.f, 0.f, 0.f }, lu[3] = { 0.f, 0.f, 0.f };
     float gw[3] = { 0.f, 0.f, 0.f };
     float du = 0.f, lp = 0.f, dbi = 0.f;
-    float su[3] = { 0.f, 0.f, 0.f }, sr = 0.f, sp = 0.f;
-    float ui_full[4];
-    Vec<D>::load(T.u, i, ui_full);  // half-step velocity incl. w
+    // a probe takes no fluid sums: its interpolated velocity, density and
+    // pressure (cfd/Sensors.cl) accumulate in gp, du and lp
     const float4 vi = a.b.velq[i];
     const float rho_i = vi.w;
     const float p_i = a.b.pmq[i].x;
@@ -487,12 +486,12 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                 du = du + udr * f_ij * rho_i / rho_j;
                 lp = lp + (p_j - p_i) * (f_ij / rho_j);
             } else if (sensor) {
-                su[0] = su[0] + vj.x * wj;
-                su[1] = su[1] + vj.y * wj;
+                gp[0] = gp[0] + vj.x * wj;
+                gp[1] = gp[1] + vj.y * wj;
                 if (D == 3)
-                    su[2] = su[2] + vj.z * wj;
-                sr = sr + rho_j * wj;
-                sp = sp + pmj.x * wj;
+                    gp[2] = gp[2] + vj.z * wj;
+                du = du + rho_j * wj;
+                lp = lp + pmj.x * wj;
             }
         } else {
             // boundary element: BIe wall sums (fluid i only)
@@ -542,15 +541,22 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
 
     // box of the positions of the lanes that take neighbours (empty when
     // none does); candidates farther than the support from it are skipped
-    float blo[3], bhi[3];
+    // (warp-uniform: kept in shared memory, read back per group, so that it
+    // holds no registers through the candidate loop)
     for (int d = 0; d < 3; d++) {
-        blo[d] = want_shep ? ri[d] : INFINITY;
-        bhi[d] = want_shep ? ri[d] : -INFINITY;
+        float lo = want_shep ? ri[d] : INFINITY;
+        float hi = want_shep ? ri[d] : -INFINITY;
         for (int o = 16; o > 0; o >>= 1) {
-            blo[d] = fminf(blo[d], __shfl_xor_sync(0xffffffffu, blo[d], o));
-            bhi[d] = fmaxf(bhi[d], __shfl_xor_sync(0xffffffffu, bhi[d], o));
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            box_s[d] = lo;
+            box_s[3 + d] = hi;
         }
     }
+    __syncwarp();
+    const volatile float* box = box_s;
     // a margin over the per-lane bound covers rounding differences between
     // the box distance and the lanes' own distances
     const float q2_box = c.q2_reject * 1.001f;
@@ -680,11 +686,11 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         if (g + lane < gend) {
             const float4 pc = grp[lane];
             const int jm = __float_as_int(pc.w);
-            const float bx = fmaxf(fmaxf(blo[0] - pc.x, pc.x - bhi[0]), 0.f);
-            const float by = fmaxf(fmaxf(blo[1] - pc.y, pc.y - bhi[1]), 0.f);
+            const float bx = fmaxf(fmaxf(box[0] - pc.x, pc.x - box[3]), 0.f);
+            const float by = fmaxf(fmaxf(box[1] - pc.y, pc.y - box[4]), 0.f);
             float bb = bx * bx + by * by;
             if (D == 3) {
-                const float bz = fmaxf(fmaxf(blo[2] - pc.z, pc.z - bhi[2]), 0.f);
+                const float bz = fmaxf(fmaxf(box[2] - pc.z, pc.z - box[5]), 0.f);
                 bb = bb + bz * bz;
             }
             cand = (jm == 1 || jm == -3) && bb < q2_box;
@@ -829,6 +835,8 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     if (a.b.shepard)
         a.b.shepard[i] = want_shep ? shep : 0.f;
 
+    float ui_full[4];
+    Vec<D>::load(T.u, i, ui_full);  // the velocity the sums used, incl. w
     float gpf[4] = { 0.f, 0.f, 0.f, 0.f }, luf[4] = { 0.f, 0.f, 0.f, 0.f };
     float gwf[4] = { 0.f, 0.f, 0.f, 0.f };
     float div_u = 0.f;
@@ -872,12 +880,12 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         for (int k = 0; k < 4; k++)
             uo[k] = ui_full[k];
         for (int k = 0; k < D; k++)
-            uo[k] = su[k];
+            uo[k] = gp[k];
         for (int k = 0; k < VS; k++)
             uo[k] = uo[k] / shp;
         Vec<D>::store(T.u, i, uo);
-        T.rho[i] = sr / shp;
-        T.p[i] = sp / shp;
+        T.rho[i] = du / shp;
+        T.p[i] = lp / shp;
     }
 
     if (im <= 0)
@@ -1042,6 +1050,7 @@ k_sweep(Consts c, StepArgs a)
     __shared__ QE s_queue[MODE == kSweepQueue ? NQ * NT : 1];
     __shared__ __align__(16) float4 s_vel[WP][2 * 32];
     __shared__ __align__(8) float2 s_pm[WP][2 * 32];
+    __shared__ float s_box[NT / 32][8];
     __shared__ uint32_t s_cstart[NT / 32][32];
     __shared__ __align__(16) float4 s_grp[NT / 32][2 * 32];
     __shared__ __align__(8) uint64_t s_mbar[NT / 32][2];
@@ -1080,7 +1089,8 @@ k_sweep(Consts c, StepArgs a)
                 c, a, valid ? cw.x + lane : cw.x, valid,
                 s_queue + (MODE == kSweepQueue ? threadIdx.x : 0),
                 s_cstart[warp], s_grp[warp], s_mbar[warp], phases,
-                s_vel[WP > 1 ? warp : 0], s_pm[WP > 1 ? warp : 0]);
+                s_vel[WP > 1 ? warp : 0], s_pm[WP > 1 ? warp : 0],
+                s_box[warp]);
             __syncwarp();  // s_cstart and s_grp are rewritten for the next chunk
             for (int o = 16; o > 0; o >>= 1)
                 v = cl_min(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -1293,7 +1303,8 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
     case 8:
         k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect><<<grid, 128, 0, s>>>(c, a);
         break;
-    // the same with the register budget of 28 or 32 resident warps per SM
+    // the same with the register budget of 28, 32, 36 or 40 resident warps
+    // per SM
     case 9:
         k_sweep<D, 64, 1, uint32_t, true, false, kSweepDirect, 28><<<grid, 64, 0, s>>>(c, a);
         break;
@@ -1305,6 +1316,18 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
         break;
     case 12:
         k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect, 32><<<grid, 128, 0, s>>>(c, a);
+        break;
+    case 13:
+        k_sweep<D, 64, 1, uint32_t, true, false, kSweepDirect, 36><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 14:
+        k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect, 36><<<grid, 128, 0, s>>>(c, a);
+        break;
+    case 15:
+        k_sweep<D, 64, 1, uint32_t, true, false, kSweepDirect, 40><<<grid, 64, 0, s>>>(c, a);
+        break;
+    case 16:
+        k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect, 40><<<grid, 128, 0, s>>>(c, a);
         break;
     default:
         k_sweep<D, 128, 128, uint16_t, false, false, kSweepQueue><<<grid, 128, 0, s>>>(c, a);
