@@ -21,15 +21,15 @@ from . import _lib
 # resident warps per SM its register budget allows); the variant numbers are
 # those of aqua_set_tuning (3 and 4 stage the candidates with bulk copies,
 # 5 and 6 sum each candidate group directly, without a queue, 7 and 8 too,
-# with the next group prefetched by asynchronous copies, 9-16 those
-# compiled for 28, 32, 36 or 40 resident warps per SM)
+# with the next group prefetched by asynchronous copies, 9-14 those
+# compiled for 28, 32 or 36 resident warps per SM)
 VARIANTS = ((0, 128, 128, 24), (1, 64, 128, 24), (2, 64, 64, 24),
             (3, 64, 128, 24), (4, 64, 64, 24), (5, 64, 0, 24), (6, 128, 0, 24),
             (7, 64, 0, 24), (8, 128, 0, 24), (9, 64, 0, 28), (10, 128, 0, 28),
             (11, 64, 0, 32), (12, 128, 0, 32), (13, 64, 0, 36),
-            (14, 128, 0, 36), (15, 64, 0, 40), (16, 128, 0, 40))
+            (14, 128, 0, 36))
 # resident warps per SM tried for each variant (blocks = warps * 32 / threads)
-WARPS_PER_SM = (8, 12, 16, 20, 24, 28, 32, 36, 40)
+WARPS_PER_SM = (8, 12, 16, 20, 24, 28, 32, 36)
 MAX_BLOCKS_PER_SM = 32
 
 

@@ -47,7 +47,7 @@ struct aqua_ctx
     int extras = 0;
     int fast = 0;              // 1: -use_fast_math step kernels
     unsigned sweep_grid = 0;   // persistent sweep blocks
-    int sweep_variant = 0;     // block size / queue depth of the sweep
+    int sweep_variant = 11;    // launch shape of the sweep (aqua_set_tuning)
     int sms = 1;
     void* pool = nullptr;
     size_t pool_bytes = 0;
@@ -144,6 +144,9 @@ build_consts(const aqua_params* p, Consts& c)
     // pairs below it take the exact test
     const double lim = (double)p->SUPPORT * (double)p->H;
     c.q2_reject = (float)(lim * lim * (1.0 + 1.0e-4));
+    c.inv_H = 1.f / p->H;
+    c.w_conw = (p->dims == 3 ? WendlandC<3>::W : WendlandC<2>::W) * p->CONW;
+    c.f_conf = (p->dims == 3 ? WendlandC<3>::F : WendlandC<2>::F) * p->CONF;
     return AQUA_OK;
 }
 
@@ -401,7 +404,8 @@ aqua_create(const aqua_params* params, uint32_t capacity,
     }
     // persistent sweep: 5 blocks of 128 threads per SM fetch chunks
     x->sms = sms > 0 ? sms : 1;
-    x->sweep_grid = (unsigned)x->sms * 5u;
+    // untuned default: the direct sweep with prefetch, 32 warps per SM
+    x->sweep_grid = (unsigned)x->sms * 16u;
     x->pool_bytes = layout(x, nullptr);
     if (cudaMalloc(&x->pool, x->pool_bytes) != cudaSuccess) {
         cudaGetLastError();

@@ -46,6 +46,10 @@ struct Consts
     float cell_length;  // support * h (LinkList.cpp:156)
     float idist;        // 1 / (support * h) (LinkList.cl.in:73)
     float q2_reject;    // |r_ij|^2 >= q2_reject  =>  |r_ij| / H >= SUPPORT
+    // folded factors of the fast build's pair sums
+    float inv_H;        // 1 / H
+    float w_conw;       // W factor of the Wendland kernel * CONW
+    float f_conf;       // F factor * CONF
 };
 
 // Device-side scalars of one case of the resident state (a batch holds

@@ -16,13 +16,30 @@ constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
 // 5 = 64 threads, 6 = 128 threads, and with the next group's records
 // prefetched by asynchronous copies: 7 = 64 threads, 8 = 128 threads;
 // those with the register budget of 28 resident warps per SM (9 = 64,
-// 10 = 128 threads), 32 (11, 12), 36 (13, 14) or 40 (15, 16)
-constexpr int kSweepVariants = 17;
+// 10 = 128 threads), 32 (11, 12) or 36 (13, 14)
+constexpr int kSweepVariants = 15;
 inline int
 sweep_variant_threads(int v)
 {
     return (v == 0 || (v >= 6 && v % 2 == 0)) ? 128 : 64;
 }
+
+// Wendland C2 (Wendland{2D,3D}.hcl:44-66): the constant factors of W and F;
+// float products folded at compile time, as the OpenCL compiler folds them
+template<int D>
+struct WendlandC;
+template<>
+struct WendlandC<3>
+{
+    static constexpr float W = 0.08203125f * 0.318309886f;
+    static constexpr float F = 0.8203125f * 0.318309886f;
+};
+template<>
+struct WendlandC<2>
+{
+    static constexpr float W = 0.109375f * 0.318309886f;
+    static constexpr float F = 1.09375f * 0.318309886f;
+};
 
 // The reference's vec type: float4 in 3-D, float2 in 2-D
 template<int D>

@@ -8,7 +8,9 @@
 namespace aqua {
 
 namespace exact {
+#define AQUA_FAST_ARITH 0
 #include "step_kernels.cuh"
+#undef AQUA_FAST_ARITH
 }  // namespace exact
 
 namespace {

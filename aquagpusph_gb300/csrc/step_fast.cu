@@ -7,6 +7,8 @@
 
 namespace aqua {
 namespace fast {
+#define AQUA_FAST_ARITH 1
 #include "step_kernels.cuh"
+#undef AQUA_FAST_ARITH
 }  // namespace fast
 }  // namespace aqua

@@ -49,6 +49,11 @@ namespace {
 
 constexpr uint32_t kBulkWaitLimit = 1u << 20;  // bounded mbarrier polls
 
+// The fast build (step_fast.cu) factors the fluid pair sums of the direct
+// sweep (reassociated, within the fast build's tolerance); the exact build
+// keeps the reference's expressions
+constexpr bool kFastArith = AQUA_FAST_ARITH != 0;
+
 // How the sweep hands in-support candidates to the pair arithmetic: per-lane
 // ring queues drained with full warps, or directly, each survivor of a group
 // summed at once by the lanes it reaches
@@ -83,23 +88,8 @@ cp_async_wait_all_but_one()
     asm volatile("cp.async.wait_group 1;\n" ::: "memory");
 }
 
-// Wendland C2 (Wendland{2D,3D}.hcl:44-66); the constants are float
-// products folded at compile time, as the OpenCL compiler folds them
-template<int D>
-struct WendlandC;
-template<>
-struct WendlandC<3>
-{
-    static constexpr float W = 0.08203125f * 0.318309886f;
-    static constexpr float F = 0.8203125f * 0.318309886f;
-};
-template<>
-struct WendlandC<2>
-{
-    static constexpr float W = 0.109375f * 0.318309886f;
-    static constexpr float F = 1.09375f * 0.318309886f;
-};
-
+// Wendland C2 kernel (Wendland{2D,3D}.hcl:44-66); constants in WendlandC
+// (kernels.cuh)
 template<int D>
 __device__ __forceinline__ float
 kernel_w(float q)
@@ -508,6 +498,76 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         }
     };
 
+    // Separation r_ij = r_j - r_i and its square (one expression for every
+    // path, so the fast build contracts it the same way everywhere)
+    auto sep = [&](const float4 pj, float& d0, float& d1, float& d2) -> float {
+        d0 = pj.x - ri[0];
+        d1 = pj.y - ri[1];
+        d2 = (D == 3) ? pj.z - ri[2] : 0.f;
+        float rr = d0 * d0 + d1 * d1;
+        if (D == 3)
+            rr = rr + d2 * d2;
+        return rr;
+    };
+    // The fast build's pair sums: vj.w carries the neighbour's volume
+    // m_j/rho_j, CONW and CONF are folded into the kernel factors, and the
+    // fluid sums leave out the factors of particle i (1/rho_i, 2/rho_i,
+    // rho_i), applied once after the loop.  The self pair adds exact zeros
+    // to every sum but Shepard's, so it takes no test.
+    auto pair_v = [&](uint32_t j, const float4 pj, const float4 vj,
+                      const float2 pmj, float d0, float d1, float d2,
+                      float rr) {
+        const int jm = __float_as_int(pj.w);
+        const float q = sqrtf(rr) * c.inv_H;
+        if (q >= c.SUPPORT)
+            return;
+        const float tq = 2.f - q;
+        const float tq2 = tq * tq;
+        const float wp = c.w_conw * (1.f + 2.f * q) * tq2 * tq2;  // W(q) CONW
+        if (jm == 1) {
+            const float wj = wp * vj.w;
+            shep = shep + wj;
+            if (fluid) {
+                const float gf = c.f_conf * tq2 * tq * vj.w;  // F(q) CONF m/rho
+                const float dv0 = vj.x - uiv[0], dv1 = vj.y - uiv[1];
+                const float dv2 = (D == 3) ? vj.z - uiv[2] : 0.f;
+                float udr = dv0 * d0 + dv1 * d1;
+                if (D == 3)
+                    udr = udr + dv2 * d2;
+                const float t = (p_i + pmj.x) * gf;
+                gp[0] = gp[0] + t * d0;
+                gp[1] = gp[1] + t * d1;
+                lu[0] = lu[0] + gf * dv0;
+                lu[1] = lu[1] + gf * dv1;
+                if (D == 3) {
+                    gp[2] = gp[2] + t * d2;
+                    lu[2] = lu[2] + gf * dv2;
+                }
+                du = du + udr * gf;
+                lp = lp + (pmj.x - p_i) * gf;
+            } else if (sensor) {
+                gp[0] = gp[0] + vj.x * wj;
+                gp[1] = gp[1] + vj.y * wj;
+                if (D == 3)
+                    gp[2] = gp[2] + vj.z * wj;
+                du = du + wp * pmj.y;  // rho_j W CONW m_j / rho_j
+                lp = lp + pmj.x * wj;
+            }
+        } else {
+            // boundary element: BIe wall sums (fluid i only)
+            float nj[3];
+            load_normal<D>(a.dst.normal, j, nj);
+            const float uj[3] = { vj.x, vj.y, vj.z };
+            const float wa = wp * pmj.y;
+            float g[3];
+            for (int kk = 0; kk < D; kk++) {
+                g[kk] = nj[kk] * wa;
+                gw[kk] = gw[kk] + g[kk];
+            }
+            dbi = dbi - dot_d<D>(uj, g);
+        }
+    };
+
     uint32_t qh = 0, qt = 0;  // ring queue head / tail
     // The drain is software-pipelined: the records of the next queued
     // neighbour are loaded while the current pair is computed.
@@ -535,7 +595,15 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
             const float2 pmj = mn;
             if (qh + 1 < upto)
                 fetch(qh + 1);
-            pair(j, pj, vj, pmj);
+            if constexpr (kFastArith) {
+                float d0, d1, d2;
+                const float rr = sep(pj, d0, d1, d2);
+                float4 vv = vj;
+                vv.w = pmj.y / vj.w;  // the volume m_j / rho_j
+                pair_v(j, pj, vv, pmj, d0, d1, d2, rr);
+            } else {
+                pair(j, pj, vj, pmj);
+            }
         }
     };
 
@@ -591,7 +659,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         return true;
     };
     auto issue = [&](int b, const uint2 se, uint32_t g) {
-        if constexpr (BULK && MODE == kSweepDirect) {
+        if constexpr (BULK && MODE != kSweepQueue) {
             // every lane copies its candidate's three records; committed by
             // the caller as one group per candidate group
             const uint32_t j = se.x + g + lane;
@@ -615,7 +683,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         }
     };
     auto wait = [&](int b) -> bool {
-        if constexpr (MODE == kSweepDirect) {
+        if constexpr (MODE != kSweepQueue) {
             // the group before the newest is this one
             cp_async_wait_all_but_one();
             __syncwarp();
@@ -640,7 +708,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     int buf = 0;
     if (BULK && have)
         issue(0, se, g);
-    if (BULK && MODE == kSweepDirect)
+    if (BULK && MODE != kSweepQueue)
         cp_async_commit();
     while (have) {
         int kn = k;
@@ -649,7 +717,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         const bool hn = advance(kn, sen, gn);
         if (BULK && hn)
             issue(buf ^ 1, sen, gn);
-        if (BULK && MODE == kSweepDirect)
+        if (BULK && MODE != kSweepQueue)
             cp_async_commit();  // possibly empty: one group per iteration
         // warp-uniform checkpoint: make room for the next 32 candidates,
         // first draining the entries every lane has (full warps)
@@ -696,7 +764,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
             cand = (jm == 1 || jm == -3) && bb < q2_box;
         }
         uint32_t bal = __ballot_sync(0xffffffffu, cand);
-        if constexpr (MODE == kSweepDirect) {
+        if constexpr (MODE != kSweepQueue) {
             // the survivors' other records (prefetched with the group, or
             // one coalesced load per lane); then every survivor, in visiting
             // order, is summed at once by the lanes whose particle it reaches
@@ -709,20 +777,28 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                 }
                 __syncwarp();
             }
+            if constexpr (kFastArith) {
+                // the survivor's volume m_j / rho_j in place of its density
+                if (cand)
+                    vel[lane].w = pm[lane].y / vel[lane].w;
+                __syncwarp();
+            }
             while (bal) {
                 const uint32_t b = __ffs(bal) - 1;
                 bal &= bal - 1;
                 const float4 pj = grp[b];
                 const int jm = __float_as_int(pj.w);
-                const float d0 = pj.x - ri[0], d1 = pj.y - ri[1];
-                float rr = d0 * d0 + d1 * d1;
-                if (D == 3) {
-                    const float d2 = pj.z - ri[2];
-                    rr = rr + d2 * d2;
+                float d0, d1, d2;
+                const float rr = sep(pj, d0, d1, d2);
+                const bool take = want_shep &&
+                                  (jm == 1 || (bie && fluid && jm == -3)) &&
+                                  rr < c.q2_reject;
+                if (take) {
+                    if constexpr (kFastArith)
+                        pair_v(se.x + g + b, pj, vel[b], pm[b], d0, d1, d2, rr);
+                    else
+                        pair(se.x + g + b, pj, vel[b], pm[b]);
                 }
-                if (want_shep && (jm == 1 || (bie && fluid && jm == -3)) &&
-                    rr < c.q2_reject)
-                    pair(se.x + g + b, pj, vel[b], pm[b]);
             }
         }
         auto consider = [&](const float4 pj, uint32_t off) {
@@ -769,6 +845,18 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         drain(qt);
     if (!valid)
         return INFINITY;
+    if constexpr (kFastArith) {
+        // the factors of particle i left out of the fluid sums
+        if (fluid) {
+            const float ir = 1.f / rho_i;
+            const float ir2 = 2.f * ir;
+            for (int kk = 0; kk < D; kk++) {
+                gp[kk] = gp[kk] * ir;
+                lu[kk] = lu[kk] * ir2;
+            }
+            du = du * rho_i;
+        }
+    }
     if constexpr (BI) {
         // BI walls: the analytic Shepard factor (BI/Shepard.cl compute) of
         // fluid particles and probes, and the wall terms of the fluid
@@ -1303,8 +1391,8 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
     case 8:
         k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect><<<grid, 128, 0, s>>>(c, a);
         break;
-    // the same with the register budget of 28, 32, 36 or 40 resident warps
-    // per SM
+    // the same with the register budget of 28, 32 or 36 resident warps per
+    // SM
     case 9:
         k_sweep<D, 64, 1, uint32_t, true, false, kSweepDirect, 28><<<grid, 64, 0, s>>>(c, a);
         break;
@@ -1322,12 +1410,6 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
         break;
     case 14:
         k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect, 36><<<grid, 128, 0, s>>>(c, a);
-        break;
-    case 15:
-        k_sweep<D, 64, 1, uint32_t, true, false, kSweepDirect, 40><<<grid, 64, 0, s>>>(c, a);
-        break;
-    case 16:
-        k_sweep<D, 128, 1, uint32_t, true, false, kSweepDirect, 40><<<grid, 128, 0, s>>>(c, a);
         break;
     default:
         k_sweep<D, 128, 128, uint16_t, false, false, kSweepQueue><<<grid, 128, 0, s>>>(c, a);

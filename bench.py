@@ -339,6 +339,10 @@ def run_ours(args):
     # ---- the other arithmetic build of the same step, same workload
     other = "exact" if args.precision == "fast" else "fast"
     sv.set_precision(other == "fast")
+    other_tuning = None
+    if not args.no_tune:
+        # each build with its own launch shape
+        other_tuning = autotune.autotune(sv, other == "fast", stream=sid)
     sv.step(3, graph=True, stream=sid)
     stream.synchronize()
     barrier()
@@ -350,8 +354,13 @@ def run_ours(args):
     ms_other = ev0.elapsed_time(ev1) / args.steps
     sv.check(stream=sid)
     sv.set_precision(args.precision == "fast")
+    if tuning is not None:
+        sv.set_tuning(tuning["variant"], tuning["blocks_per_sm"])
     other_line = {"precision": other, "ms_per_step": ms_other,
                   "value": world * c.N / (ms_other * 1e-3)}
+    if other_tuning is not None:
+        other_line["tuning"] = {k: other_tuning[k] for k in
+                                ("variant", "blocks_per_sm", "ms_per_step")}
 
     # ---- per-stage CUDA events (same graphs with event nodes), K steps
     sv.set_profiling(True)

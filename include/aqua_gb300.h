@@ -216,7 +216,7 @@ aqua_status aqua_set_precision(aqua_ctx* ctx, int mode);
  * as it is loaded, without a queue (5: 64 threads, 6: 128 threads; 7: 64
  * and 8: 128 threads with the next group prefetched by asynchronous
  * copies; 9: 64 and 10: 128 threads of those compiled for 28 resident warps
- * per SM, 11 and 12 for 32, 13 and 14 for 36, 15 and 16 for 40);
+ * per SM, 11 and 12 for 32, 13 and 14 for 36);
  * `blocks_per_sm` the persistent grid (blocks per SM, <= 32).
  * Any choice gives the same results; aquagpusph_gb300.autotune picks the
  * fastest for a case by timing them. */

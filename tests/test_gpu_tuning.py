@@ -44,7 +44,7 @@ def run(c, variant, blocks, steps=3, fast=False):
 
 SHAPES = [(0, 2), (0, 5), (1, 10), (2, 4), (3, 8), (4, 12), (5, 10), (5, 3),
           (6, 6), (7, 12), (7, 2), (8, 6), (9, 14), (10, 7), (11, 16),
-          (12, 8), (13, 18), (14, 9), (15, 20), (16, 10)]
+          (12, 8), (13, 18), (14, 9)]
 
 
 @pytest.mark.parametrize("fast", [False, True])
