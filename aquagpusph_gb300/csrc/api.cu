@@ -47,7 +47,7 @@ struct aqua_ctx
     int extras = 0;
     int fast = 0;              // 1: -use_fast_math step kernels
     unsigned sweep_grid = 0;   // persistent sweep blocks
-    int sweep_variant = 11;    // launch shape of the sweep (aqua_set_tuning)
+    int sweep_variant = 9;     // launch shape of the sweep (aqua_set_tuning)
     int sms = 1;
     void* pool = nullptr;
     size_t pool_bytes = 0;
@@ -404,8 +404,8 @@ aqua_create(const aqua_params* params, uint32_t capacity,
     }
     // persistent sweep: 5 blocks of 128 threads per SM fetch chunks
     x->sms = sms > 0 ? sms : 1;
-    // untuned default: the direct sweep with prefetch, 32 warps per SM
-    x->sweep_grid = (unsigned)x->sms * 16u;
+    // untuned default: the direct sweep with prefetch, 28 warps per SM
+    x->sweep_grid = (unsigned)x->sms * 14u;
     x->pool_bytes = layout(x, nullptr);
     if (cudaMalloc(&x->pool, x->pool_bytes) != cudaSuccess) {
         cudaGetLastError();

@@ -1362,8 +1362,9 @@ launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
     if (a.N == 0)
         return cudaSuccess;
     if (c.boundary == AQUA_BOUNDARY_BI) {
-        // one launch shape for the BI walls
-        k_sweep<D, 64, 128, uint16_t, false, true, kSweepQueue><<<grid, 64, 0, s>>>(c, a);
+        // one launch shape for the BI walls: the direct sweep with prefetch
+        // and the register budget of 28 resident warps per SM
+        k_sweep<D, 64, 1, uint32_t, true, true, kSweepDirect, 28><<<grid, 64, 0, s>>>(c, a);
         return cudaGetLastError();
     }
     switch (variant) {
