@@ -16,15 +16,19 @@ namespace exact {
 namespace {
 
 // Cell-aligned chunks of <= 32 sorted particles: s starts a chunk when it is
-// 0, 32, 64, ... particles past the first particle of its cell.
-__global__ void __launch_bounds__(256)
+// 0, 32, 64, ... particles past the first particle of its cell.  One
+// atomicAdd per block of 1024 reserves the block's chunks (in sorted order
+// within the block), so the shared counter sees few atomics.
+constexpr int kChunkThreads = 1024;
+__global__ void __launch_bounds__(kChunkThreads)
 k_chunks(const uint32_t* skeys, const uint2* cells, uint32_t N, uint2* chunks,
          DevScalars* sc)
 {
+    __shared__ uint32_t s_count[kChunkThreads / 32];
     if (sc->err)
         return;
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     bool start = false;
     uint2 w = make_uint2(0, 0);
     if (s < N) {
@@ -33,12 +37,29 @@ k_chunks(const uint32_t* skeys, const uint2* cells, uint32_t N, uint2* chunks,
         w = make_uint2(s, min(32u, se.y - s));
     }
     const unsigned b = __ballot_sync(0xffffffffu, start);
-    uint32_t base = 0;
-    if (lane == 0 && b)
-        base = atomicAdd(&sc->n_chunks, (uint32_t)__popc(b));
-    base = __shfl_sync(0xffffffffu, base, 0);
+    if (lane == 0)
+        s_count[warp] = __popc(b);
+    __syncthreads();
+    if (warp == 0) {
+        // exclusive scan of the warps' counts, one reservation for the block
+        const uint32_t v = lane < kChunkThreads / 32 ? s_count[lane] : 0u;
+        uint32_t incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += t;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint32_t base = 0;
+        if (lane == 0 && total)
+            base = atomicAdd(&sc->n_chunks, total);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (lane < kChunkThreads / 32)
+            s_count[lane] = base + incl - v;
+    }
+    __syncthreads();
     if (start)
-        chunks[base + __popc(b & ((1u << lane) - 1u))] = w;
+        chunks[s_count[warp] + __popc(b & ((1u << lane) - 1u))] = w;
 }
 
 // End of step of every case: dt = min(dt_var) (Reduction tool), assert
@@ -198,8 +219,8 @@ launch_sweep(bool fast, const Consts& c, const StepArgs& a, unsigned grid,
              int variant, cudaStream_t s)
 {
     if (a.N) {
-        k_chunks<<<(a.N + 255) / 256, 256, 0, s>>>(a.skeys, a.b.cells, a.N,
-                                                    a.b.chunks, a.sc);
+        k_chunks<<<(a.N + kChunkThreads - 1) / kChunkThreads, kChunkThreads, 0,
+                   s>>>(a.skeys, a.b.cells, a.N, a.b.chunks, a.sc);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;
