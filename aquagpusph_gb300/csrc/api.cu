@@ -206,7 +206,7 @@ layout(aqua_ctx* x, char* base)
     b.digit_total = cv.take<uint32_t>(256);
     b.cells = cv.take<uint2>(x->ncap);
     b.chunks = cv.take<uint2>(n);
-    b.cell_wall = cv.take<uint8_t>(x->ncap);
+    b.wall_range = cv.take<uint2>(x->ncap);
     b.id_sorted = cv.take<uint32_t>(n);
     b.r_in = cv.take<float>((size_t)n * VS);
     b.u_in = cv.take<float>((size_t)n * VS);
@@ -257,7 +257,7 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     const uint32_t N = x->N;
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[0], s, cudaEventRecordExternal));
-    AQ_CUDA(launch_begin(x->sc, x->cs, x->n_cases, b.cells, b.cell_wall,
+    AQ_CUDA(launch_begin(x->sc, x->cs, x->n_cases, b.cells, b.wall_range,
                          x->ncap, N, s));
     if (x->dims == 3) {
         AQ_CUDA(launch_minmax<3>(x->consts, S.r, S.imove, S.cid, N, x->cs,
@@ -863,7 +863,7 @@ aqua_linklist(aqua_ctx* x, const float* r_in, uint32_t N, uint32_t* icell,
     DevScalars hs;
     std::memset(&hs, 0, sizeof(hs));
     AQ_CUDA(cudaMemcpyAsync(x->sc_aux, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
-    AQ_CUDA(launch_begin(x->sc_aux, x->cs_aux, 1, b.cells, b.cell_wall, 0, N, s));
+    AQ_CUDA(launch_begin(x->sc_aux, x->cs_aux, 1, b.cells, b.wall_range, 0, N, s));
     if (x->dims == 3) {
         AQ_CUDA(launch_minmax<3>(x->consts, r_in, nullptr, nullptr, N, x->cs_aux,
                                  x->sc_aux, s));

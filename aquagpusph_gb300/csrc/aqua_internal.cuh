@@ -121,7 +121,8 @@ struct StepBufs
     uint32_t* digit_total; // per-pass digit totals (256)
     uint2* cells;          // (start, end) per cell; (N, N) if empty
     uint2* chunks;         // (first, count) sweep chunks (<= N)
-    uint8_t* cell_wall;    // 1 if the cell holds a boundary element
+    uint2* wall_range;     // first and one past the last sorted index of the
+                           // cell's boundary elements; (~0, 0) if none
     uint32_t* id_sorted;   // old -> new
     // sorted start-of-step Variables (the reference's *_in after the
     // midpoint backups)

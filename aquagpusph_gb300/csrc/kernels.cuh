@@ -82,7 +82,7 @@ struct Vec<2>
 // link-list / sort launchers (linklist.cu).  `cid` (case of each particle)
 // may be NULL: every particle then belongs to case 0.
 cudaError_t launch_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases,
-                         uint2* cells, uint8_t* cell_wall, uint32_t ncap,
+                         uint2* cells, uint2* wall_range, uint32_t ncap,
                          uint32_t N, cudaStream_t s);
 template<int D>
 cudaError_t launch_minmax(const Consts& c, const float* r, const int32_t* imove,

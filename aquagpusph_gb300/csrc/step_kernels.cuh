@@ -379,8 +379,11 @@ k_gather(Consts c, StepArgs a)
     a.b.posq[s] = make_float4(r[0], r[1], D == 3 ? r[2] : 0.f, __int_as_float(im));
     a.b.velq[s] = make_float4(uh[0], uh[1], D == 3 ? uh[2] : 0.f, rho_h);
     a.b.pmq[s] = make_float2(p, m);
-    if (im == -3)
-        a.b.cell_wall[key] = 1;
+    if (im == -3) {
+        // the cell's boundary elements lie within [x, y) of its particles
+        atomicMin(&a.b.wall_range[key].x, s);
+        atomicMax(&a.b.wall_range[key].y, s + 1);
+    }
 }
 
 // ------------------------------------------------------------------- sweep
@@ -868,9 +871,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         bool self_added = false;
         for (int k = 0; k < NC; k++) {
             const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
-            if (!a.b.cell_wall[cn])
-                continue;
-            const uint2 se = a.b.cells[cn];
+            const uint2 se = a.b.wall_range[cn];  // empty: x > y
             for (uint32_t j = se.x; j < se.y; j++) {
                 const float4 pj = a.b.posq[j];
                 if (__float_as_int(pj.w) != -3)
@@ -1003,9 +1004,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                 vh[k] = uin[k] + hdt * acc[k];
             for (int k = 0; k < NC; k++) {
                 const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
-                if (!a.b.cell_wall[cn])
-                    continue;
-                const uint2 se = a.b.cells[cn];
+                const uint2 se = a.b.wall_range[cn];  // empty: x > y
                 for (uint32_t j = se.x; j < se.y; j++) {
                     const float4 pj = a.b.posq[j];
                     if (__float_as_int(pj.w) != -3)
@@ -1083,9 +1082,7 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         const float Ri = 0.5f * powf(T.m[i] / rho_n, 1.f / c.DIMS);
         for (int k = 0; k < NC; k++) {
             const uint32_t cn = neighbour_cell<D>(key_i, k, nx, nxy);
-            if (!a.b.cell_wall[cn])
-                continue;
-            const uint2 se = a.b.cells[cn];
+            const uint2 se = a.b.wall_range[cn];  // empty: x > y
             for (uint32_t j = se.x; j < se.y; j++) {
                 const float4 pj = a.b.posq[j];
                 if (__float_as_int(pj.w) != -3)
