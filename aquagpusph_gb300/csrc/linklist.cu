@@ -109,9 +109,10 @@ k_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases, uint2* cells,
 }
 
 // r_min / r_max of every case over its particles.  Cases are contiguous
-// runs of particles, so warps are almost always single-case: a warp reduces
-// its lanes and keeps a running box while its tiles stay in one case,
-// issuing the atomics only when the case changes and at the end.
+// runs of particles, so warps are almost always single-case: each lane keeps
+// a running box while the warp's tiles stay in one case, and the warp
+// reduces its lanes and issues the atomics only when the case changes and
+// at the end.
 template<int D>
 __global__ void __launch_bounds__(256)
 k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
@@ -122,18 +123,29 @@ k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
         return;
     const int lane = threadIdx.x & 31;
     bool bad = false;
+    // per-lane running box of the warp's current case wk (warp-uniform);
+    // min and max are exact, so the order of accumulation does not matter
     float wmn[VS], wmx[VS];
-    uint32_t wk = 0xffffffffu;  // case of the running box (warp-uniform)
+    uint32_t wk = 0xffffffffu;
     for (int d = 0; d < VS; d++) {
         wmn[d] = INFINITY;
         wmx[d] = -INFINITY;
     }
     auto flush = [&]() {
-        if (lane == 0 && wk != 0xffffffffu)
-            for (int d = 0; d < VS; d++) {
+        if (wk == 0xffffffffu)
+            return;
+        for (int d = 0; d < VS; d++) {
+            for (int o = 16; o > 0; o >>= 1) {
+                wmn[d] = cl_min(wmn[d], __shfl_xor_sync(0xffffffffu, wmn[d], o));
+                wmx[d] = cl_max(wmx[d], __shfl_xor_sync(0xffffffffu, wmx[d], o));
+            }
+            if (lane == 0) {
                 atomic_min_float(&cs[wk].r_min[d], wmn[d]);
                 atomic_max_float(&cs[wk].r_max[d], wmx[d]);
             }
+            wmn[d] = INFINITY;
+            wmx[d] = -INFINITY;
+        }
     };
     // grid-stride over warp-sized tiles so that a warp's lanes are adjacent
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
@@ -159,24 +171,13 @@ k_minmax(Consts c, const float* r, const int32_t* imove, const uint32_t* cid,
         const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
         const bool uniform = __all_sync(0xffffffffu, k == k0 || !valid);
         if (uniform) {
-            for (int d = 0; d < VS; d++) {
-                for (int o = 16; o > 0; o >>= 1) {
-                    mn[d] = cl_min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
-                    mx[d] = cl_max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
-                }
-            }
             if (k0 != wk) {
                 flush();
                 wk = k0;
-                for (int d = 0; d < VS; d++) {
-                    wmn[d] = mn[d];
-                    wmx[d] = mx[d];
-                }
-            } else {
-                for (int d = 0; d < VS; d++) {
-                    wmn[d] = cl_min(wmn[d], mn[d]);
-                    wmx[d] = cl_max(wmx[d], mx[d]);
-                }
+            }
+            for (int d = 0; d < VS; d++) {
+                wmn[d] = cl_min(wmn[d], mn[d]);
+                wmx[d] = cl_max(wmx[d], mx[d]);
             }
         } else if (valid) {
             for (int d = 0; d < VS; d++) {
