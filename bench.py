@@ -40,7 +40,7 @@ UNIT = "particle-steps/s"
 
 # Algorithmic bytes per particle (3-D, V = 16 B):
 #   whole step  B = 19 V + 96 + 20 P (P = 3 radix passes)     = 460 B
-#   fused sweep = SURVEY rows S5 + S6: read r,u,rho,m,imove,normal (3V+12),
+#   fused sweep = sweep + integrator: read r,u,rho,m,imove,normal (3V+12),
 #                 write dudt,drhodt (V+4); read r,u,rho,dudt,drhodt (3V+8),
 #                 write r,u,rho (2V+4)                          = 9V + 28
 STEP_BYTES_3D = 19 * 16 + 96 + 20 * 3

@@ -6,8 +6,8 @@ reference-kernel harness: with the midpoint scheme
 
 The analytic Shepard factor goes through atan (2-D) and acos (3-D), whose
 last bits differ between CUDA and the host libm, so after the link-list
-(compared bit for bit) the Variables are compared with the tolerance the
-north star states, 1e-5 relative to each field's largest magnitude, after
+(compared bit for bit) the Variables are compared with the per-step rate
+tolerance, 1e-5 relative to each field's largest magnitude, after
 one step, and 1e-4 after five (reordered by particle id)."""
 import dataclasses
 import os

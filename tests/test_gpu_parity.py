@@ -8,7 +8,7 @@ rounding per operation -- except positions, which go through powf in the
 BIe PST (PST.cl: 0.5*pow(m/rho, 1/DIMS)), whose last bit may differ between
 CUDA's powf and the host libm: positions are compared with
 rtol = 1e-6 (RTOL_R) and everything derived from them after further steps
-with the tolerance the benchmark spec states, 1e-5 relative (RTOL_RATES).
+with the per-step rate tolerance, 1e-5 relative (RTOL_RATES).
 """
 import os
 
