@@ -80,50 +80,68 @@ def test_free_surface_matches_restatement(gpu, dims):
     sv.close()
 
 
-def test_probe_and_free_surface_histories_within_2_percent(gpu, tmp_path):
+HIST_STATIONS = {"H1": 0.3, "H2": 1.5, "H3": 2.4}
+HIST_T_END = 0.45
+
+
+def history_case():
+    c = cases.dam_break_2d(extra_probes=[(0.0, 0.05), (1.5, 0.0)])
+    c.dt = c.params.dt_fixed
+    return c
+
+
+@pytest.fixture(scope="module")
+def oracle_history():
+    """The oracle's probe-pressure and free-surface histories of the run."""
+    c = history_case()
+    first = c.N - 3
+    orc = O.load_oracle()
+    st = O.OracleState(c)
+    p_orc, h_orc, t_orc = [], [], []
+    while st["t"] < HIST_T_END:
+        orc.step(st)
+        t_orc.append(st["t"])
+        p_orc.append(O.probe_values(st, "p", first, 3))
+        h_orc.append(O.free_surface(st, list(HIST_STATIONS.values()), 0.01, 2))
+    return (np.array(p_orc), np.array(h_orc), np.array(t_orc, np.float64))
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_probe_and_free_surface_histories_within_2_percent(gpu, tmp_path,
+                                                           oracle_history,
+                                                           fast):
     """2-D dam break (dx = 0.01, c0 = 45), from rest until the front reaches
     the far end of the tank (t = 0.45 s): the pressure histories of probes at
     the bottom of the left wall and on the bottom at x = 1.5 m (wetted by the
     front), and the free-surface elevation at three stations, from the GPU
-    run (reports written in the reference's formats) and from the oracle
-    stepped on the same input.  Each history agrees with the oracle's within
-    2% in relative L2 norm over the run.  (Pointwise, the pressure at the
-    instant the front reaches a probe is timing sensitive: a spike a few
-    steps early or late exceeds 2% of the peak while the histories agree.)
+    run (reports written in the reference's formats; exact and fast builds)
+    and from the oracle stepped on the same input.  Each history agrees with
+    the oracle's within 2% in relative L2 norm over the run.  (Pointwise, the
+    pressure at the instant the front reaches a probe is timing sensitive: a
+    spike a few steps early or late exceeds 2% of the peak while the
+    histories agree.)
 
     Past the impact on the right wall (t > 0.6 s) the flow is chaotic at this
     resolution: two oracle runs whose inputs differ by one ulp in one
     particle position drift apart as far as the GPU run and the oracle do, so
     the window ends before it."""
-    c = cases.dam_break_2d(extra_probes=[(0.0, 0.05), (1.5, 0.0)])
-    c.dt = c.params.dt_fixed
+    c = history_case()
     first = c.N - 3          # right wall (y = 0.16), left wall, bottom
-    stations = {"H1": 0.3, "H2": 1.5, "H3": 2.4}
-    t_end = 0.45
+    stations = HIST_STATIONS
 
-    sv = solver(c)
+    sv = solver(c, fast=fast)
     probes = R.SetTabFile(str(tmp_path / "sensors.out"), "p, shepard",
                           first=first, n=3, ipf=1)
     hfile = R.TabFile(str(tmp_path / "sensors_h.out"), ["t"] + list(stations))
     run = R.Run(sv, [probes], R.FreeSurfaceSensors(stations, 0.01), hfile)
-    steps = run.advance(end_time=t_end)
+    steps = run.advance(end_time=HIST_T_END)
     run.close()
     sv.close()
     t_gpu, cols = R.read_set_tab_file(str(tmp_path / "sensors.out"))
     assert len(t_gpu) == steps
     p_gpu = np.stack([cols[f"p_{first + k}"] for k in range(3)], 1)
     h_gpu = np.array([[r[k] for k in stations] for r in hfile.rows])
-
-    orc = O.load_oracle()
-    st = O.OracleState(c)
-    p_orc, h_orc, t_orc = [], [], []
-    while st["t"] < t_end:
-        orc.step(st)
-        t_orc.append(st["t"])
-        p_orc.append(O.probe_values(st, "p", first, 3))
-        h_orc.append(O.free_surface(st, list(stations.values()), 0.01, 2))
-    p_orc, h_orc = np.array(p_orc), np.array(h_orc)
-    t_orc = np.array(t_orc, np.float64)
+    p_orc, h_orc, t_orc = oracle_history
 
     def l2(a, b):
         nb = np.linalg.norm(b)
