@@ -51,17 +51,23 @@ make_idesc(uint32_t n)
            ((uint32_t)(kTcRows >> 4) << 24);
 }
 
+// SiLU as z * sigmoid(z) with sigmoid(z) = (1 + tanh(z / 2)) / 2 on the
+// hardware tanh (tanh.approx.f32, about 2^-11 relative error): well below
+// the bf16 rounding of the activation that follows
 __device__ __forceinline__ float
 silu_f(float z)
 {
-    return z / (1.f + expf(-z));
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+    return z * fmaf(0.5f, t, 0.5f);
 }
 
+// two floats rounded to bf16 (round to nearest even), lo in the low half
 __device__ __forceinline__ uint32_t
 pack2(float lo, float hi)
 {
-    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
-           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
 }
 
 // copy a rows x K bf16 block (row-major, ld elements) into the core-matrix
@@ -202,7 +208,259 @@ k_linear_fwd_tc(uint32_t M, uint32_t K, const uint16_t* __restrict__ X,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fused three-layer edge MLP: Y = L3(act(L2(act(L1(X))))) on tiles of 128
+// edges, every activation kept on chip.  The layer-1 input of each tile is
+// gathered into shared memory (core-matrix layout) by asynchronous copies:
+// rows of X, or, in PAIR mode, the concatenation [H[recv[e]] (64),
+// H[send[e]] (64), Ef[e] (16)] that aqua_gnn_gather_pair materialises.  The
+// three layers share one 64-column tensor-memory accumulator; each epilogue
+// reads it back (tcgen05.ld), adds the bias, applies the activation, rounds
+// to BF16 and writes the next layer's A operand into shared memory, exactly
+// the values the unfused layers store to and reload from global memory, so
+// the result is bit-identical to three aqua_gnn_linear_fwd_tc calls.  Only
+// the BF16 output of layer 3 is written.
+
+__device__ __forceinline__ void
+cp_async_16z(void* dst, const void* src, bool valid)
+{
+    // src-size 0 fills the 16 bytes with zeros
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(valid ? 16u : 0u)
+                 : "memory");
+}
+
+template<int K1, bool PAIR>
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
+              const uint32_t* __restrict__ recv, const uint32_t* __restrict__ send,
+              const uint16_t* __restrict__ H, uint32_t ldh,
+              const uint16_t* __restrict__ Ef,
+              const uint16_t* __restrict__ W1, const float* __restrict__ b1,
+              const uint16_t* __restrict__ W2, const float* __restrict__ b2,
+              const uint16_t* __restrict__ W3, const float* __restrict__ b3,
+              int act1, int act2, int act3, uint16_t* Y, uint32_t ldy, int* err)
+{
+    constexpr uint32_t kW1 = ((64u * K1 * 2u + 1023u) / 1024u) * 1024u;
+    constexpr uint32_t kW = 64u * 64u * 2u;            // W2, W3
+    constexpr uint32_t kA0 = ((128u * K1 * 2u + 1023u) / 1024u) * 1024u;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sW1 = smem;
+    uint8_t* sW2 = sW1 + kW1;
+    uint8_t* sW3 = sW2 + kW;
+    uint8_t* sA0 = sW3 + kW;
+    uint8_t* sA1 = sA0 + kA0;                          // 128 x 64
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    stage(sW1, W1, K1, 64, 64, K1);
+    stage(sW2, W2, 64, 64, 64, 64);
+    stage(sW3, W3, 64, 64, 64, 64);
+    if (threadIdx.x == 0)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_addr(&mbar)));
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 "
+                     "[%0], %1;\n" :: "r"(smem_addr(&tmem_base)), "r"(64u));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = make_idesc(64);
+    uint32_t phase = 0;
+    bool failed = false;
+
+    // issue the MMAs of one layer (thread 0) and wait for them (everyone)
+    auto layer = [&](const uint8_t* sA, const uint8_t* sB, uint32_t K) -> bool {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            const uint32_t sbo = (K / 8) * 128;
+            for (uint32_t ks = 0; ks < K / 16; ks++) {
+                const uint64_t ad = make_desc(smem_addr(sA) + ks * 256, 128, sbo);
+                const uint64_t bd = make_desc(smem_addr(sB) + ks * 256, 128, sbo);
+                const uint32_t acc = ks > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                    :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one."
+                         "shared::cluster.b64 [%0];\n" :: "r"(smem_addr(&mbar)));
+        }
+        uint32_t done = 0;
+        for (uint32_t it = 0; it < kWaitLimit && !done; it++) {
+            asm volatile("{\n.reg .pred p;\n"
+                         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                         "selp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(done) : "r"(smem_addr(&mbar)), "r"(phase));
+        }
+        bool bad = !__all_sync(0xffffffffu, done);
+        if (bad && lane == 0)
+            atomicExch(err, 1);
+        bad = __syncthreads_or(bad);
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        return !bad;
+    };
+    // read the accumulator row of this thread, add the bias, activate;
+    // `emit(g, packed8)` receives the row's k-group g (8 bf16 as a uint4)
+    auto epilogue = [&](const float* __restrict__ bias, int act, auto&& emit) {
+        const uint32_t taddr = tmem + ((warp * 32u) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+                  "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+                  "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                  "=r"(v[14]), "=r"(v[15])
+                : "r"(taddr + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+            uint32_t p[8];
+            for (int j = 0; j < 8; j++) {
+                float z0 = __uint_as_float(v[2 * j]) + bias[c0 + 2 * j];
+                float z1 = __uint_as_float(v[2 * j + 1]) + bias[c0 + 2 * j + 1];
+                if (act == AQUA_ACT_SILU) {
+                    z0 = silu_f(z0);
+                    z1 = silu_f(z1);
+                }
+                p[j] = pack2(z0, z1);
+            }
+            emit(c0 / 8, make_uint4(p[0], p[1], p[2], p[3]));
+            emit(c0 / 8 + 1, make_uint4(p[4], p[5], p[6], p[7]));
+        }
+    };
+    const uint32_t r = threadIdx.x;  // this thread's row of the tile
+    auto to_a1 = [&](int g, uint4 val) {
+        *reinterpret_cast<uint4*>(sA1 + ((r / 8) * 8 + g) * 128 + (r % 8) * 16) = val;
+    };
+
+    const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
+    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const uint32_t e = tile * kTcRows + r;
+        const bool valid = e < E;
+        // layer-1 input rows, gathered asynchronously into sA0
+        constexpr uint32_t kg = K1 / 8;
+        uint8_t* row0 = sA0 + (r / 8) * kg * 128 + (r % 8) * 16;
+        if (PAIR) {
+            const uint32_t er = valid ? recv[e] : 0u, es = valid ? send[e] : 0u;
+            for (uint32_t g = 0; g < kg; g++) {
+                const uint16_t* src =
+                    g < 8 ? H + (size_t)er * ldh + g * 8
+                          : (g < 16 ? H + (size_t)es * ldh + (g - 8) * 8
+                                    : Ef + (size_t)(valid ? e : 0u) * 16 + (g - 16) * 8);
+                cp_async_16z(row0 + g * 128, src, valid);
+            }
+        } else {
+            for (uint32_t g = 0; g < kg; g++)
+                cp_async_16z(row0 + g * 128, X + (size_t)(valid ? e : 0u) * ldx + g * 8,
+                             valid);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        if (!layer(sA0, sW1, K1)) {
+            failed = true;
+            break;
+        }
+        epilogue(b1, act1, to_a1);
+        if (!layer(sA1, sW2, 64)) {
+            failed = true;
+            break;
+        }
+        epilogue(b2, act2, to_a1);
+        if (!layer(sA1, sW3, 64)) {
+            failed = true;
+            break;
+        }
+        epilogue(b3, act3, [&](int g, uint4 val) {
+            if (valid)
+                *reinterpret_cast<uint4*>(Y + (size_t)e * ldy + g * 8) = val;
+        });
+        // the next tile's copies and MMAs reuse sA0, sA1 and the accumulator
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncthreads();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n"
+                     :: "r"(tmem), "r"(64u));
+    }
+}
+
+template<int K1, bool PAIR>
+constexpr size_t
+edge_mlp_smem()
+{
+    return ((64u * K1 * 2u + 1023u) / 1024u) * 1024u + 2u * 64u * 64u * 2u +
+           ((128u * K1 * 2u + 1023u) / 1024u) * 1024u + 128u * 64u * 2u;
+}
+
 }  // namespace
+
+extern "C" aqua_status
+aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
+                     const uint32_t* recv, const uint32_t* send,
+                     const uint16_t* H, uint32_t ldh, const uint16_t* Ef,
+                     const uint16_t* W1, const float* b1, const uint16_t* W2,
+                     const float* b2, const uint16_t* W3, const float* b3,
+                     int32_t act1, int32_t act2, int32_t act3, uint16_t* Y,
+                     uint32_t ldy, int32_t* err, void* stream)
+{
+    auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+    const bool pair = (X == nullptr);
+    if (!W1 || !b1 || !W2 || !b2 || !W3 || !b3 || !Y || !err || ldy < 64 ||
+        ldy % 8 || !a16(Y) || !a16(W1) || !a16(W2) || !a16(W3))
+        return AQUA_ERR_INVALID;
+    if (pair) {
+        if (K1 != 144 || !recv || !send || !H || !Ef || ldh < 64 || ldh % 8 ||
+            !a16(H) || !a16(Ef))
+            return AQUA_ERR_INVALID;
+    } else if (K1 != AQUA_GNN_FEATURES || ldx < K1 || ldx % 8 || !a16(X)) {
+        return AQUA_ERR_INVALID;
+    }
+    if (E == 0)
+        return AQUA_OK;
+    static bool configured = false;
+    if (!configured) {
+        if (cudaFuncSetAttribute(k_edge_mlp_tc<16, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)edge_mlp_smem<16, false>()) != cudaSuccess ||
+            cudaFuncSetAttribute(k_edge_mlp_tc<144, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)edge_mlp_smem<144, true>()) != cudaSuccess)
+            return AQUA_ERR_CUDA;
+        configured = true;
+    }
+    int sms = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+            cudaSuccess)
+        return AQUA_ERR_CUDA;
+    const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (pair) {
+        // 88 KB of shared memory: two CTAs per SM (128 of 512 TMEM columns)
+        const uint32_t grid = tiles < (uint32_t)sms * 2u ? tiles : (uint32_t)sms * 2u;
+        k_edge_mlp_tc<144, true><<<grid, kTcThreads, edge_mlp_smem<144, true>(), s>>>(
+            E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
+            act1, act2, act3, Y, ldy, err);
+    } else {
+        // 39 KB: at most five CTAs per SM (320 TMEM columns)
+        const uint32_t grid = tiles < (uint32_t)sms * 5u ? tiles : (uint32_t)sms * 5u;
+        k_edge_mlp_tc<16, false><<<grid, kTcThreads, edge_mlp_smem<16, false>(), s>>>(
+            E, X, ldx, nullptr, nullptr, nullptr, 0, nullptr, W1, b1, W2, b2, W3,
+            b3, act1, act2, act3, Y, ldy, err);
+    }
+    return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
+}
 
 extern "C" aqua_status
 aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N, const uint16_t* X,

@@ -41,6 +41,9 @@ AGG_SCALE = 1.0 / 32.0
 # 64-wide layers run on tcgen05 (tensor memory) when True, on mma.sync
 # otherwise (the 16-wide output layer always uses mma.sync)
 USE_TCGEN05 = True
+# inference runs each edge MLP as one fused tcgen05 kernel (inputs gathered
+# and activations kept on chip) when True
+FUSE_EDGE_MLP = True
 
 _vp = C.c_void_p
 
@@ -82,6 +85,9 @@ SIGNATURES = {
                                 _u32, _i32, _vp],
         "aqua_gnn_linear_fwd_tc": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32,
                                _vp, _u32, _i32, _vp, _vp],
+        "aqua_gnn_edge_mlp_tc": [_u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32, _vp,
+                                 _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32,
+                                 _vp, _u32, _vp, _vp],
     "aqua_gnn_linear_dgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _u32, _i32,
                                   _vp, _u32, _vp],
         "aqua_gnn_linear_wgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _u32, _vp, _vp, _vp],
@@ -339,12 +345,13 @@ class Network:
     """Forward (and, with ``train``, backward) of the model on one graph."""
 
     def __init__(self, model: Model, graph: Graph, inputs: Inputs, stream=None,
-                 tcgen05=None):
+                 tcgen05=None, fused=None):
         torch = _torch()
         self.model, self.g, self.x = model, graph, inputs
         self.s = _vp(stream or 0)
         self.stream = stream
         self.tc = USE_TCGEN05 if tcgen05 is None else bool(tcgen05)
+        self.fused = self.tc and (FUSE_EDGE_MLP if fused is None else bool(fused))
         self.err = torch.zeros(1, dtype=torch.int32, device=graph.rs.device)
 
     def _buf(self, shape, dtype):
@@ -388,6 +395,26 @@ class Network:
                     self._lin(name, cur, ldc, M, _vp(0), 0, out, ldo)
         return A, Z
 
+    def _edge_mlp_fused(self, prefix, E, X=None, ldx=0, H=None, ldh=0, Ef=None):
+        """The three layers of an edge MLP in one tcgen05 kernel (inference:
+        no activations kept); returns the E x 64 bf16 output."""
+        torch = _torch()
+        m = self.model
+        y = self._buf((max(E, 1), 64), torch.bfloat16)
+        names = [f"{prefix}_{k}" for k in range(3)]
+        acts = [m.offs[nm][4] for nm in names]
+        k1 = m.offs[names[0]][3]
+        g = self.g
+        _chk("aqua_gnn_edge_mlp_tc", lib().aqua_gnn_edge_mlp_tc(
+            E, k1, X or _vp(0), ldx,
+            _p(g.receivers) if H is not None else _vp(0),
+            _p(g.senders) if H is not None else _vp(0),
+            H or _vp(0), ldh, Ef or _vp(0),
+            m.W(names[0]), m.b(names[0]), m.W(names[1]), m.b(names[1]),
+            m.W(names[2]), m.b(names[2]), acts[0], acts[1], acts[2],
+            _p(y), 64, _p(self.err), self.s))
+        return y
+
     def forward(self, train=False):
         torch = _torch()
         L = lib()
@@ -400,7 +427,11 @@ class Network:
             E, dims, _p(g.receivers), _p(g.senders), _p(x.r), _p(x.u), _p(x.rho),
             _p(x.imove), _p(x.normal), _p(m.scales), _p(E0), s))
         c["E0"] = E0
-        A, Z = self._mlp("e1", _p(E0), FEAT, E, train)
+        fused = self.fused and not train
+        if fused:
+            A, Z = [self._edge_mlp_fused("e1", E, X=_p(E0), ldx=FEAT)], []
+        else:
+            A, Z = self._mlp("e1", _p(E0), FEAT, E, train)
         c["e1"] = (A, Z)
         n1_in = self._buf((n, 80), torch.bfloat16)
         _chk("aqua_gnn_segment_sum", L.aqua_gnn_segment_sum(
@@ -413,11 +444,15 @@ class Network:
         H = _vp(n2_in.data_ptr() + 2 * 64)
         A, Z = self._mlp("n1", _p(n1_in), 80, n, train, out=H, ldo=144)
         c["n1"] = (A, Z)
-        X2 = self._buf((max(E, 1), 144), torch.bfloat16)
-        _chk("aqua_gnn_gather_pair", L.aqua_gnn_gather_pair(
-            E, _p(g.receivers), _p(g.senders), H, 144, _p(E0), _p(X2), s))
-        c["X2"] = X2
-        A, Z = self._mlp("e2", _p(X2), 144, E, train)
+        if fused:
+            # the pair inputs are gathered on chip: X2 is never built
+            A, Z = [self._edge_mlp_fused("e2", E, H=H, ldh=144, Ef=_p(E0))], []
+        else:
+            X2 = self._buf((max(E, 1), 144), torch.bfloat16)
+            _chk("aqua_gnn_gather_pair", L.aqua_gnn_gather_pair(
+                E, _p(g.receivers), _p(g.senders), H, 144, _p(E0), _p(X2), s))
+            c["X2"] = X2
+            A, Z = self._mlp("e2", _p(X2), 144, E, train)
         c["e2"] = (A, Z)
         _chk("aqua_gnn_segment_sum", L.aqua_gnn_segment_sum(
             n, _p(g.offsets), _p(A[-1]), 64, AGG_SCALE, _p(n2_in), 144, 0, s))

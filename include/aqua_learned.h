@@ -123,6 +123,24 @@ aqua_status aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N,
                                    const uint16_t* W, const float* b, float* Z,
                                    uint32_t ldz, uint16_t* Y, uint32_t ldy,
                                    int32_t act, int32_t* err, void* stream);
+/* A whole three-layer edge MLP on the tensor cores, activations on chip:
+ * Y = L3(act3)(L2(act2)(L1(act1)(X))), 64-wide layers (W1: 64 x K1, W2, W3:
+ * 64 x 64, bf16; biases f32), Y: E x 64 bf16 at ldy.  The layer-1 input is
+ * the rows of X (K1 = AQUA_GNN_FEATURES, ldx) or, with X = NULL, the
+ * concatenation [H[recv[e]], H[send[e]], Ef[e]] (K1 = 144) that
+ * aqua_gnn_gather_pair builds -- gathered on chip instead.  Bit-identical to
+ * three aqua_gnn_linear_fwd_tc calls with the intermediate activations
+ * rounded to bf16.  A time-out of the bounded waits sets *err. */
+aqua_status aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X,
+                                 uint32_t ldx, const uint32_t* recv,
+                                 const uint32_t* send, const uint16_t* H,
+                                 uint32_t ldh, const uint16_t* Ef,
+                                 const uint16_t* W1, const float* b1,
+                                 const uint16_t* W2, const float* b2,
+                                 const uint16_t* W3, const float* b3,
+                                 int32_t act1, int32_t act2, int32_t act3,
+                                 uint16_t* Y, uint32_t ldy, int32_t* err,
+                                 void* stream);
 /* dX = dY W (M x K, bf16 at ldx) where dY: M x N bf16 (ldy), Wt: K x N.
  * With Zprev (M x K f32, ldzp) and act_prev = AQUA_ACT_SILU the result is
  * multiplied by silu'(Zprev) (the gradient of the previous layer's

@@ -216,3 +216,21 @@ def test_proposal_judge_and_rollback(torch):
     assert st["proposals"] == 3 and st["judged"] == 6
     assert 0 <= st["rolled_back"] <= 6
     sv.close()
+
+
+def test_fused_edge_mlps_equal_the_layer_by_layer_forward(torch):
+    """Inference with each edge MLP as one fused tcgen05 kernel gives the
+    layer-by-layer tcgen05 forward bit for bit."""
+    from aquagpusph_gb300 import learned as Lm
+    b = small_batch(3)
+    sv, g, x, host = network_inputs(torch, b)
+    params = Lm.init_params(11)
+    model = Lm.Model(2, params)
+    model.scales.copy_(torch.tensor((float(b.case.params.h), 0.05, 0.5, 0.5,
+                                     5.0, 998.0)))
+    outs = []
+    for fused in (False, True):
+        net = Lm.Network(model, g, x, tcgen05=True, fused=fused)
+        outs.append(net.forward(train=False).clone())
+    assert torch.equal(outs[0], outs[1])
+    sv.close()

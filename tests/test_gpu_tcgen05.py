@@ -56,3 +56,96 @@ def test_tcgen05_forward_matches(torch, M, K):
     # the two tensor-core paths agree to within one bf16 rounding
     y2 = Y2.float().cpu().numpy()
     assert np.abs(y1 - y2).max() <= 2.0 ** -7 * max(np.abs(y2).max(), 1)
+
+
+def three_layers(torch, Lm, L, X, K, Ws, bs, acts, err):
+    """Three aqua_gnn_linear_fwd_tc calls, bf16 activations in between."""
+    cur, ldc = X, K
+    for W, b, act in zip(Ws, bs, acts):
+        y = torch.empty((X.shape[0], 64), dtype=torch.bfloat16, device="cuda")
+        assert L.aqua_gnn_linear_fwd_tc(X.shape[0], ldc, 64, Lm._p(cur), ldc,
+                                        Lm._p(W), Lm._p(b), None, 0, Lm._p(y),
+                                        64, act, Lm._p(err), None) == 0
+        cur, ldc = y, 64
+    return cur
+
+
+def weights(torch, rng, K1):
+    Ws, bs = [], []
+    for k in (K1, 64, 64):
+        W = G.bf16(rng.normal(0, 0.2, (64, k)).astype(np.float32))
+        Ws.append(torch.from_numpy(W).cuda().to(torch.bfloat16))
+        bs.append(torch.from_numpy(rng.normal(0, 0.1, 64).astype(np.float32)).cuda())
+    return Ws, bs
+
+
+@pytest.mark.parametrize("E", [1, 127, 128, 1000, 100000])
+def test_fused_edge_mlp_rows_equals_three_layers(torch, E):
+    """Layer-1 input from rows (the first round's edge features)."""
+    from aquagpusph_gb300 import learned as Lm
+    L = Lm.lib()
+    rng = np.random.default_rng(E)
+    X = torch.from_numpy(G.bf16(rng.normal(0, 1, (E, 16)).astype(np.float32))
+                         ).cuda().to(torch.bfloat16)
+    Ws, bs = weights(torch, rng, 16)
+    acts = (1, 1, 0)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ref = three_layers(torch, Lm, L, X, 16, Ws, bs, acts, err)
+    Y = torch.empty((E, 64), dtype=torch.bfloat16, device="cuda")
+    assert L.aqua_gnn_edge_mlp_tc(E, 16, Lm._p(X), 16, None, None, None, 0, None,
+                                  Lm._p(Ws[0]), Lm._p(bs[0]), Lm._p(Ws[1]),
+                                  Lm._p(bs[1]), Lm._p(Ws[2]), Lm._p(bs[2]),
+                                  *acts, Lm._p(Y), 64, Lm._p(err), None) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert torch.equal(Y.view(torch.int16), ref.view(torch.int16))
+
+
+@pytest.mark.parametrize("E,n", [(1, 3), (300, 40), (100000, 2500)])
+def test_fused_edge_mlp_pairs_equals_gather_and_three_layers(torch, E, n):
+    """Layer-1 input gathered on chip from the node latents of both ends and
+    the edge features ([H[recv], H[send], Ef], as aqua_gnn_gather_pair)."""
+    from aquagpusph_gb300 import learned as Lm
+    L = Lm.lib()
+    rng = np.random.default_rng(E + n)
+    node = G.bf16(rng.normal(0, 1, (n, 144)).astype(np.float32))
+    nd = torch.from_numpy(node).cuda().to(torch.bfloat16)
+    H = Lm._vp(nd.data_ptr() + 2 * 64)   # columns 64..127 of rows 144 apart
+    Ef = torch.from_numpy(G.bf16(rng.normal(0, 1, (E, 16)).astype(np.float32))
+                          ).cuda().to(torch.bfloat16)
+    recv = torch.from_numpy(np.sort(rng.integers(0, n, E)).astype(np.uint32)
+                            .view(np.int32)).cuda()
+    send = torch.from_numpy(rng.integers(0, n, E).astype(np.uint32)
+                            .view(np.int32)).cuda()
+    X2 = torch.empty((E, 144), dtype=torch.bfloat16, device="cuda")
+    assert L.aqua_gnn_gather_pair(E, Lm._p(recv), Lm._p(send), H, 144,
+                                  Lm._p(Ef), Lm._p(X2), None) == 0
+    Ws, bs = weights(torch, rng, 144)
+    acts = (1, 1, 0)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ref = three_layers(torch, Lm, L, X2, 144, Ws, bs, acts, err)
+    Y = torch.empty((E, 64), dtype=torch.bfloat16, device="cuda")
+    assert L.aqua_gnn_edge_mlp_tc(E, 144, None, 0, Lm._p(recv), Lm._p(send), H,
+                                  144, Lm._p(Ef), Lm._p(Ws[0]), Lm._p(bs[0]),
+                                  Lm._p(Ws[1]), Lm._p(bs[1]), Lm._p(Ws[2]),
+                                  Lm._p(bs[2]), *acts, Lm._p(Y), 64, Lm._p(err),
+                                  None) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert torch.equal(Y.view(torch.int16), ref.view(torch.int16))
+
+
+def test_fused_edge_mlp_rejects_bad_arguments(torch):
+    from aquagpusph_gb300 import learned as Lm
+    L = Lm.lib()
+    W = torch.zeros((64, 64), dtype=torch.bfloat16, device="cuda")
+    b = torch.zeros(64, dtype=torch.float32, device="cuda")
+    Y = torch.empty((8, 64), dtype=torch.bfloat16, device="cuda")
+    X = torch.zeros((8, 32), dtype=torch.bfloat16, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    args = [Lm._p(W), Lm._p(b)] * 3 + [1, 1, 0, Lm._p(Y), 64, Lm._p(err), None]
+    # rows input must have K1 = 16; pair input needs its index arrays
+    assert L.aqua_gnn_edge_mlp_tc(8, 32, Lm._p(X), 32, None, None, None, 0, None,
+                                  *args) == -1
+    assert L.aqua_gnn_edge_mlp_tc(8, 144, None, 0, None, None, None, 144, None,
+                                  *args) == -1
