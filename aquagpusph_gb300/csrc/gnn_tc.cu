@@ -243,15 +243,16 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
 {
     constexpr uint32_t kW1 = ((64u * K1 * 2u + 1023u) / 1024u) * 1024u;
     constexpr uint32_t kW = 64u * 64u * 2u;            // W2, W3
-    constexpr uint32_t kA0 = ((128u * K1 * 2u + 1023u) / 1024u) * 1024u;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     uint8_t* sW1 = smem;
     uint8_t* sW2 = sW1 + kW1;
     uint8_t* sW3 = sW2 + kW;
+    // one operand buffer: the layer-1 input (128 x K1), then, once layer 1's
+    // MMAs have completed, the 128 x 64 activations of layers 1 and 2
     uint8_t* sA0 = sW3 + kW;
-    uint8_t* sA1 = sA0 + kA0;                          // 128 x 64
+    uint8_t* sA1 = sA0;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     stage(sW1, W1, K1, 64, 64, K1);
@@ -399,8 +400,10 @@ template<int K1, bool PAIR>
 constexpr size_t
 edge_mlp_smem()
 {
+    constexpr size_t a0 = ((128u * K1 * 2u + 1023u) / 1024u) * 1024u;
+    constexpr size_t a1 = 128u * 64u * 2u;
     return ((64u * K1 * 2u + 1023u) / 1024u) * 1024u + 2u * 64u * 64u * 2u +
-           ((128u * K1 * 2u + 1023u) / 1024u) * 1024u + 128u * 64u * 2u;
+           (a0 > a1 ? a0 : a1);
 }
 
 }  // namespace
@@ -447,14 +450,14 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
     const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
     cudaStream_t s = (cudaStream_t)stream;
     if (pair) {
-        // 88 KB of shared memory: two CTAs per SM (128 of 512 TMEM columns)
-        const uint32_t grid = tiles < (uint32_t)sms * 2u ? tiles : (uint32_t)sms * 2u;
+        // 72 KB of shared memory: three CTAs per SM (192 of 512 TMEM columns)
+        const uint32_t grid = tiles < (uint32_t)sms * 3u ? tiles : (uint32_t)sms * 3u;
         k_edge_mlp_tc<144, true><<<grid, kTcThreads, edge_mlp_smem<144, true>(), s>>>(
             E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
             act1, act2, act3, Y, ldy, err);
     } else {
-        // 39 KB: at most five CTAs per SM (320 TMEM columns)
-        const uint32_t grid = tiles < (uint32_t)sms * 5u ? tiles : (uint32_t)sms * 5u;
+        // 34 KB: at most six CTAs per SM (384 TMEM columns)
+        const uint32_t grid = tiles < (uint32_t)sms * 6u ? tiles : (uint32_t)sms * 6u;
         k_edge_mlp_tc<16, false><<<grid, kTcThreads, edge_mlp_smem<16, false>(), s>>>(
             E, X, ldx, nullptr, nullptr, nullptr, 0, nullptr, W1, b1, W2, b2, W3,
             b3, act1, act2, act3, Y, ldy, err);
