@@ -101,7 +101,8 @@ def test_fused_edge_mlp_rows_equals_three_layers(torch, E):
     assert torch.equal(Y.view(torch.int16), ref.view(torch.int16))
 
 
-@pytest.mark.parametrize("E,n", [(1, 3), (300, 40), (100000, 2500)])
+@pytest.mark.parametrize("E,n", [(1, 3), (300, 40), (100000, 2500),
+                                 (1000000, 25000)])
 def test_fused_edge_mlp_pairs_equals_gather_and_three_layers(torch, E, n):
     """Layer-1 input gathered on chip from the node latents of both ends and
     the edge features ([H[recv], H[send], Ef], as aqua_gnn_gather_pair)."""
