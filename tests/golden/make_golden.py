@@ -22,10 +22,15 @@ GPU host included, can check against them).
 * step_ie_{2d,3d}.npz -- BI walls with the improved Euler scheme
   (basic/time_scheme/improved_euler.xml in place of the midpoint scheme, as
   in the reference's BI examples), after one, two and five steps.
+* history_3d.npz -- the probe-pressure history of the CPU oracle (the
+  restatement the reference kernels pin) over a small 3-D dam break (0.6 x
+  0.2 x 0.4 m tank, 0.2 m water cube, dx = 0.01 m, 15,602 particles) from
+  rest through the impact on the far wall, to t = 0.3 s (6,001 steps):
+  the oracle takes minutes for it, so the GPU test reads it from here.
 
-    python tests/golden/make_golden.py [/path/to/reference] [bi|ie]
+    python tests/golden/make_golden.py [/path/to/reference] [bi|ie|history]
 
-regenerates everything, or only the BI or improved-Euler fixtures.
+regenerates everything, or only the BI, improved-Euler or history fixtures.
 """
 import os
 import sys
@@ -139,17 +144,46 @@ def make_steps_bi(scheme=0):
         np.savez_compressed(os.path.join(HERE, f"{name}_{dims}d.npz"), **data)
 
 
+def history_case_3d():
+    c = cases.dam_break_3d(dx=0.01, tank=(0.6, 0.2, 0.4), block=(0.2, 0.2, 0.2),
+                           probes_z=(0.02, 0.06))
+    c.dt = c.params.dt_fixed
+    return c
+
+
+HISTORY_T_END = 0.3
+
+
+def make_history_3d():
+    c = history_case_3d()
+    first = c.N - 2
+    orc = O.load_oracle()
+    st = O.OracleState(c)
+    ts, ps = [], []
+    while st["t"] < HISTORY_T_END:
+        orc.step(st)
+        ts.append(st["t"])
+        ps.append(O.probe_values(st, "p", first, 2))
+    np.savez_compressed(os.path.join(HERE, "history_3d.npz"),
+                        t=np.array(ts, np.float64), p=np.array(ps, np.float32),
+                        n=np.int64(c.N), first=np.int64(first))
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     O.build_oracle(ref=True)
     if len(sys.argv) > 2 and sys.argv[2] in ("bi", "ie"):
         make_steps_bi(1 if sys.argv[2] == "ie" else 0)
         return
+    if len(sys.argv) > 2 and sys.argv[2] == "history":
+        make_history_3d()
+        return
     make_linklist(ref_root)
     make_radixsort(ref_root)
     make_steps()
     make_steps_bi()
     make_steps_bi(scheme=1)
+    make_history_3d()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
