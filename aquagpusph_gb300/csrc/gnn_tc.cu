@@ -14,6 +14,7 @@
 // Every wait on the mbarrier is bounded: on time-out the kernel records
 // an error, skips the tile's stores, frees its TMEM and returns.
 #include <cuda_bf16.h>
+#include <atomic>
 #include <cstdint>
 
 #include "aqua_learned.h"
@@ -431,8 +432,15 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
     }
     if (E == 0)
         return AQUA_OK;
-    static bool configured = false;
-    if (!configured) {
+    int sms = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+            cudaSuccess)
+        return AQUA_ERR_CUDA;
+    // the shared-memory limit is a per-device attribute of each kernel
+    static std::atomic<uint64_t> configured{ 0 };
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (!bit || !(configured.load() & bit)) {
         if (cudaFuncSetAttribute(k_edge_mlp_tc<16, false>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)edge_mlp_smem<16, false>()) != cudaSuccess ||
@@ -440,13 +448,8 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)edge_mlp_smem<144, true>()) != cudaSuccess)
             return AQUA_ERR_CUDA;
-        configured = true;
+        configured.fetch_or(bit);
     }
-    int sms = 0, dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
-            cudaSuccess)
-        return AQUA_ERR_CUDA;
     const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
     cudaStream_t s = (cudaStream_t)stream;
     if (pair) {
@@ -486,19 +489,20 @@ aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N, const uint16_t* X,
     // tensor-memory columns), so tcgen05.alloc never has to wait
     if (bytes < 30 * 1024)
         bytes = 30 * 1024;
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(k_linear_fwd_tc<64>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 64 * 1024) != cudaSuccess)
-            return AQUA_ERR_CUDA;
-        configured = true;
-    }
     int sms = 0, dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
             cudaSuccess)
         return AQUA_ERR_CUDA;
+    static std::atomic<uint64_t> configured{ 0 };
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (!bit || !(configured.load() & bit)) {
+        if (cudaFuncSetAttribute(k_linear_fwd_tc<64>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 64 * 1024) != cudaSuccess)
+            return AQUA_ERR_CUDA;
+        configured.fetch_or(bit);
+    }
     const uint32_t tiles = (M + kTcRows - 1) / kTcRows;
     const uint32_t grid = tiles < (uint32_t)sms * 8u ? tiles : (uint32_t)sms * 8u;
     k_linear_fwd_tc<64><<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
