@@ -53,6 +53,14 @@ struct aqua_ctx
     size_t pool_bytes = 0;
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t graph[2] = { nullptr, nullptr };
+    // configuration the graphs were captured for (particles, cases, roll)
+    uint32_t graph_n = 0, graph_cases = 0;
+    int graph_motion = -1;
+    // pinned staging areas of the small host -> device copies (case scalars,
+    // motions, offsets): one for aqua_set_state, one for aqua_set_cases, each
+    // reused once its event shows the copies that last read it executed
+    uint8_t* stage[2] = { nullptr, nullptr };
+    cudaEvent_t stage_ev[2] = { nullptr, nullptr };
     // stage boundary events (recorded when profiling is on): before the
     // link-list, before the gather, before the sweep, after the sweep, end
     static constexpr int kEvents = 5;
@@ -246,6 +254,33 @@ drop_graphs(aqua_ctx* x)
     }
 }
 
+// Layout of the pinned staging area: the step scalars, then per-case
+// scalars, motions and offsets for up to kMaxCases cases
+constexpr size_t kStageCs = 256;
+constexpr size_t kStageCm = kStageCs + ((kMaxCases * sizeof(CaseScalars) + 255) & ~(size_t)255);
+constexpr size_t kStageOff = kStageCm + ((kMaxCases * sizeof(CaseMotion) + 255) & ~(size_t)255);
+constexpr size_t kStageBytes = kStageOff + (kMaxCases + 1) * sizeof(uint32_t);
+
+// Staging area `slot` for the next small copies: waits (if at all) for the
+// copies that last read it, so that the host may overwrite it.  The copies
+// themselves stay asynchronous; stage_done() marks their position in the
+// stream.
+constexpr int kStageState = 0;  // aqua_set_state
+constexpr int kStageCases = 1;  // aqua_set_cases
+
+uint8_t*
+stage_begin(aqua_ctx* x, int slot)
+{
+    return cudaEventSynchronize(x->stage_ev[slot]) == cudaSuccess ? x->stage[slot]
+                                                                  : nullptr;
+}
+
+cudaError_t
+stage_done(aqua_ctx* x, int slot, cudaStream_t s)
+{
+    return cudaEventRecord(x->stage_ev[slot], s);
+}
+
 // Launches one step on `s` (the resident state advances from set[cur] to
 // set[cur ^ 1]; the caller flips cur).
 aqua_status
@@ -402,7 +437,6 @@ aqua_create(const aqua_params* params, uint32_t capacity,
         delete x;
         return AQUA_ERR_CUDA;
     }
-    // persistent sweep: 5 blocks of 128 threads per SM fetch chunks
     x->sms = sms > 0 ? sms : 1;
     // untuned default: the direct sweep with prefetch, 28 warps per SM
     x->sweep_grid = (unsigned)x->sms * 14u;
@@ -421,9 +455,14 @@ aqua_create(const aqua_params* params, uint32_t capacity,
         }
     if (cudaMemset(x->pool, 0, x->pool_bytes) != cudaSuccess ||
         cudaStreamCreateWithFlags(&x->cap_stream, cudaStreamNonBlocking) !=
+            cudaSuccess ||
+        cudaMallocHost(&x->stage[0], kStageBytes) != cudaSuccess ||
+        cudaMallocHost(&x->stage[1], kStageBytes) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->stage_ev[0], cudaEventDisableTiming) !=
+            cudaSuccess ||
+        cudaEventCreateWithFlags(&x->stage_ev[1], cudaEventDisableTiming) !=
             cudaSuccess) {
-        cudaFree(x->pool);
-        delete x;
+        aqua_destroy(x);
         return AQUA_ERR_CUDA;
     }
     *out = x;
@@ -441,6 +480,14 @@ aqua_destroy(aqua_ctx* x)
     for (int k = 0; k < aqua_ctx::kEvents; k++)
         if (x->ev[k])
             cudaEventDestroy(x->ev[k]);
+    for (int k = 0; k < 2; k++) {
+        if (x->stage_ev[k]) {
+            cudaEventSynchronize(x->stage_ev[k]);  // no copy still reads it
+            cudaEventDestroy(x->stage_ev[k]);
+        }
+        if (x->stage[k])
+            cudaFreeHost(x->stage[k]);
+    }
     if (x->pool)
         cudaFree(x->pool);
     delete x;
@@ -514,31 +561,35 @@ aqua_set_state(aqua_ctx* x, uint32_t N, const aqua_vars* v, int on_host,
     AQ_TRY(copy_in(d.drhodt, v->drhodt, N * 4ull, on_host, s));
     AQ_TRY(copy_in(d.m, v->m, N * 4ull, on_host, s));
     AQ_TRY(copy_in(d.p, v->p, N * 4ull, on_host, s));
-    if (N != x->N)
-        drop_graphs(x);
     x->N = N;
-    DevScalars hs;
-    std::memset(&hs, 0, sizeof(hs));
-    AQ_CUDA(cudaMemcpyAsync(x->sc, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
-    // one case holding every particle (aqua_set_cases() splits them)
-    CaseScalars c0;
-    std::memset(&c0, 0, sizeof(c0));
-    c0.t = t;
-    c0.dt = dt;
-    c0.iter = iter;
-    c0.dt_next = 0x7f800000u;
-    c0.cos_psi = c0.cos_psi_in = 1.f;
-    CaseMotion m0;
-    std::memset(&m0, 0, sizeof(m0));
-    const uint32_t off[2] = { 0u, N };
+    // the step scalars and one case holding every particle (aqua_set_cases()
+    // splits them), through the pinned staging area: asynchronous
+    uint8_t* st = stage_begin(x, kStageState);
+    if (!st)
+        return AQUA_ERR_CUDA;
+    DevScalars* hs = reinterpret_cast<DevScalars*>(st);
+    CaseScalars* c0 = reinterpret_cast<CaseScalars*>(st + kStageCs);
+    CaseMotion* m0 = reinterpret_cast<CaseMotion*>(st + kStageCm);
+    uint32_t* off = reinterpret_cast<uint32_t*>(st + kStageOff);
+    std::memset(hs, 0, sizeof(*hs));
+    std::memset(c0, 0, sizeof(*c0));
+    c0->t = t;
+    c0->dt = dt;
+    c0->iter = iter;
+    c0->dt_next = 0x7f800000u;
+    c0->cos_psi = c0->cos_psi_in = 1.f;
+    std::memset(m0, 0, sizeof(*m0));
+    off[0] = 0u;
+    off[1] = N;
     x->n_cases = 1;
     x->has_motion = 0;
-    // pageable sources: the copies complete before the call returns
-    AQ_CUDA(cudaMemcpyAsync(x->cs, &c0, sizeof(c0), cudaMemcpyHostToDevice, s));
-    AQ_CUDA(cudaMemcpyAsync(x->cm, &m0, sizeof(m0), cudaMemcpyHostToDevice, s));
-    AQ_CUDA(cudaMemcpyAsync(x->offsets, off, sizeof(off), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(cudaMemcpyAsync(x->sc, hs, sizeof(*hs), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(cudaMemcpyAsync(x->cs, c0, sizeof(*c0), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(cudaMemcpyAsync(x->cm, m0, sizeof(*m0), cudaMemcpyHostToDevice, s));
+    AQ_CUDA(cudaMemcpyAsync(x->offsets, off, 2 * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, s));
+    AQ_CUDA(stage_done(x, kStageState, s));
     AQ_CUDA(launch_set_case_ids(x->set[x->cur].cid, x->offsets, 1, N, s));
-    AQ_CUDA(cudaStreamSynchronize(s));
     return AQUA_OK;
 }
 
@@ -704,13 +755,14 @@ aqua_set_cases(aqua_ctx* x, uint32_t n_cases, const uint32_t* offsets,
         if (offsets[k + 1] < offsets[k])
             return AQUA_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
-    CaseScalars* hs = new (std::nothrow) CaseScalars[n_cases];
-    CaseMotion* hm = new (std::nothrow) CaseMotion[n_cases];
-    if (!hs || !hm) {
-        delete[] hs;
-        delete[] hm;
-        return AQUA_ERR_NO_MEMORY;
-    }
+    // the per-case records are built in the pinned staging area and copied
+    // asynchronously
+    uint8_t* st = stage_begin(x, kStageCases);
+    if (!st)
+        return AQUA_ERR_CUDA;
+    CaseScalars* hs = reinterpret_cast<CaseScalars*>(st + kStageCs);
+    CaseMotion* hm = reinterpret_cast<CaseMotion*>(st + kStageCm);
+    uint32_t* ho = reinterpret_cast<uint32_t*>(st + kStageOff);
     int motion = 0;
     for (uint32_t k = 0; k < n_cases; k++) {
         std::memset(&hs[k], 0, sizeof(CaseScalars));
@@ -737,20 +789,19 @@ aqua_set_cases(aqua_ctx* x, uint32_t n_cases, const uint32_t* offsets,
         hs[k].sin_psi_in = hs[k].sin_psi;
         motion |= hm[k].enabled;
     }
+    std::memcpy(ho, offsets, (n_cases + 1) * sizeof(uint32_t));
     cudaError_t e = cudaMemcpyAsync(x->cs, hs, n_cases * sizeof(CaseScalars),
                                     cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(x->cm, hm, n_cases * sizeof(CaseMotion),
                             cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(x->offsets, offsets, (n_cases + 1) * sizeof(uint32_t),
+        e = cudaMemcpyAsync(x->offsets, ho, (n_cases + 1) * sizeof(uint32_t),
                             cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
-        e = launch_set_case_ids(x->set[x->cur].cid, x->offsets, n_cases, x->N, s);
+        e = stage_done(x, kStageCases, s);
     if (e == cudaSuccess)
-        e = cudaStreamSynchronize(s);
-    delete[] hs;
-    delete[] hm;
+        e = launch_set_case_ids(x->set[x->cur].cid, x->offsets, n_cases, x->N, s);
     if (e != cudaSuccess) {
         std::fprintf(stderr, "aqua_gb300: aqua_set_cases failed: %s\n",
                      cudaGetErrorString(e));
@@ -758,7 +809,6 @@ aqua_set_cases(aqua_ctx* x, uint32_t n_cases, const uint32_t* offsets,
     }
     x->n_cases = n_cases;
     x->has_motion = motion;
-    drop_graphs(x);
     return AQUA_OK;
 }
 
@@ -776,6 +826,14 @@ aqua_step(aqua_ctx* x, uint32_t nsteps, int use_graph, void* stream)
     if (!x || x->N == 0)
         return AQUA_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
+    if (use_graph && (x->graph_n != x->N || x->graph_cases != x->n_cases ||
+                      x->graph_motion != x->has_motion)) {
+        // the launches depend on these: capture again
+        drop_graphs(x);
+        x->graph_n = x->N;
+        x->graph_cases = x->n_cases;
+        x->graph_motion = x->has_motion;
+    }
     for (uint32_t k = 0; k < nsteps; k++) {
         if (!use_graph) {
             AQ_TRY(enqueue_step(x, x->cur, s));

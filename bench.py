@@ -404,16 +404,24 @@ def run_ours(args):
     d2h = sum(t.numel() for t in outs[0].values())
     e2e_steps = 2 * max(1, min(args.steps, 10) // 2)
     ctxs = ((sv, sid), (sv2, sid2))
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
+
+    def e2e_round_trip(k):
         s_, sid_ = ctxs[k % 2]
         s_.set_state_raw(c.N, addr_in, True, c.t, c.dt, c.iter, stream=sid_)
         if batch:
             s_.set_cases(batch, stream=sid_)
         s_.step(1, graph=True, stream=sid_)
         s_.get_state_raw(addr_out[k % 2], True, stream=sid_)
+
+    # one untimed round trip per context (the stage profiling above dropped
+    # the main context's graphs: they are captured here, not in the timing)
+    for k in range(2):
+        e2e_round_trip(k)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        e2e_round_trip(k)
     stream.synchronize()
     stream2.synchronize()
     e2e_s = time.perf_counter() - t0

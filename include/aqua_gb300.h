@@ -225,9 +225,12 @@ aqua_status aqua_set_tuning(aqua_ctx* ctx, uint32_t sweep_variant,
 
 /* Uploads the particle Variables of an N-particle case into the resident
  * state (the ParticlesSet loaders, FileManager.cpp:136-139).  `on_host` = 1
- * for host pointers (pinned memory makes the copies asynchronous), 0 for
- * device pointers.  Required fields: id, iset, imove, r, normal, tangent, u,
- * dudt, rho, drhodt, m, p.  binormal may be NULL.  Also sets t, dt, iter. */
+ * for host pointers, 0 for device pointers.  The call does not synchronise:
+ * from pinned host memory the copies run asynchronously on `stream`, so the
+ * buffers must stay unchanged until the stream has executed them (pageable
+ * buffers are staged before the call returns).  Required fields: id, iset,
+ * imove, r, normal, tangent, u, dudt, rho, drhodt, m, p.  binormal may be
+ * NULL.  Also sets t, dt, iter. */
 aqua_status aqua_set_state(aqua_ctx* ctx, uint32_t N, const aqua_vars* src,
                            int on_host, float t, float dt, uint32_t iter,
                            void* stream);
