@@ -114,19 +114,27 @@ class Solver:
         self.set_cases(batch, stream)
 
     def set_cases(self, batch, stream=None):
-        """The case split of a Batch whose particles are already resident."""
-        n = len(batch.offsets) - 1
-        offs = np.ascontiguousarray(batch.offsets, np.uint32)
-        arr = (_lib.AquaCase * n)()
-        for k, m in enumerate(batch.motions):
-            a = arr[k]
-            a.t, a.dt, a.iter = batch.case.t, batch.case.dt, batch.case.iter
-            if m is not None:
-                a.roll_enabled = 1
-                a.roll_iset = m.iset
-                a.roll_amplitude = m.amplitude
-                a.roll_angular_freq = m.angular_freq
-                a.roll_center[:] = (list(m.center) + [0.0] * 4)[:4]
+        """The case split of a Batch whose particles are already resident.
+        The case records are built once per Batch and (t, dt, iter) and
+        reused on later calls."""
+        key = (id(batch), batch.case.t, batch.case.dt, batch.case.iter)
+        cached = getattr(self, "_cases_cache", None)
+        if cached is None or cached[0] != key or cached[1] is not batch:
+            n = len(batch.offsets) - 1
+            offs = np.ascontiguousarray(batch.offsets, np.uint32)
+            arr = (_lib.AquaCase * n)()
+            for k, m in enumerate(batch.motions):
+                a = arr[k]
+                a.t, a.dt, a.iter = batch.case.t, batch.case.dt, batch.case.iter
+                if m is not None:
+                    a.roll_enabled = 1
+                    a.roll_iset = m.iset
+                    a.roll_amplitude = m.amplitude
+                    a.roll_angular_freq = m.angular_freq
+                    a.roll_center[:] = (list(m.center) + [0.0] * 4)[:4]
+            cached = (key, batch, n, offs, arr)
+            self._cases_cache = cached
+        _, _, n, offs, arr = cached
         _lib.check("aqua_set_cases", self.lib.aqua_set_cases(
             self.ctx, n, offs.ctypes.data_as(_lib._U), arr,
             C.c_void_p(stream or 0)))

@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -402,7 +403,10 @@ def run_ours(args):
     addr_out = [{k: t.data_ptr() for k, t in o.items()} for o in outs]
     h2d = sum(t.numel() for t in host.values())
     d2h = sum(t.numel() for t in outs[0].values())
-    e2e_steps = 2 * max(1, min(args.steps, 10) // 2)
+    # about 0.2 s of device work (at least K steps, at most 200), so that
+    # host jitter does not dominate short steps
+    e2e_steps = max(args.steps, int(math.ceil(200.0 / max(ms_step, 1e-3))))
+    e2e_steps = 2 * max(1, min(e2e_steps, 200) // 2)
     ctxs = ((sv, sid), (sv2, sid2))
 
     def e2e_round_trip(k):
