@@ -115,6 +115,9 @@ class AquaScalars(C.Structure):
 # (name, restype, argtypes) of every function include/aqua_gb300.h declares
 SIGNATURES = [
     ("aqua_version", C.c_char_p, []),
+    ("aqua_malloc", C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
+    ("aqua_free", C.c_int, [C.c_void_p]),
+    ("aqua_memcpy", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]),
     ("aqua_create", C.c_int, [C.POINTER(AquaParams), C.c_uint32, C.c_uint32,
                               C.POINTER(C.c_void_p)]),
     ("aqua_destroy", C.c_int, [C.c_void_p]),

@@ -410,6 +410,45 @@ aqua_version(void)
 }
 
 aqua_status
+aqua_malloc(void** ptr, size_t bytes)
+{
+    if (!ptr || bytes == 0)
+        return AQUA_ERR_INVALID;
+    *ptr = nullptr;
+    if (cudaMalloc(ptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return AQUA_ERR_NO_MEMORY;
+    }
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_free(void* ptr)
+{
+    if (ptr)
+        AQ_CUDA(cudaFree(ptr));
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_memcpy(void* dst, const void* src, size_t bytes, int kind)
+{
+    if ((!dst || !src) && bytes)
+        return AQUA_ERR_INVALID;
+    cudaMemcpyKind k;
+    switch (kind) {
+    case AQUA_COPY_H2D: k = cudaMemcpyHostToDevice; break;
+    case AQUA_COPY_D2H: k = cudaMemcpyDeviceToHost; break;
+    case AQUA_COPY_D2D: k = cudaMemcpyDeviceToDevice; break;
+    default: return AQUA_ERR_INVALID;
+    }
+    if (bytes)
+        AQ_CUDA(cudaMemcpy(dst, src, bytes, k));
+    return AQUA_OK;
+}
+
+aqua_status
 aqua_create(const aqua_params* params, uint32_t capacity,
             uint32_t ihoc_capacity, aqua_ctx** out)
 {

@@ -1,16 +1,19 @@
-// libaqua_cuda_tool.so -- an installable tool that runs the canonical WCSPH
-// step on the GPU through the aqua_gb300 C ABI.  It has the shape of the
-// reference's installable-tool example (tests/ExternalTool/tool.{hpp,cpp}:
-// a Tool subclass plus a C-linkage create_object(name, once) factory), so a
-// step loop can name it <Tool type="installable" path="libaqua_cuda_tool.so">
-// in place of the tools from "predictor" to "iter += 1" (basic.xml:132-171
-// with the midpoint, domain, cfd, deltaSPH, BIe and variableTimeStep
-// presets).
+// libaqua_cuda_tool.so -- installable tools that run the canonical WCSPH
+// step, or only its link-list, on the GPU through the aqua_gb300 C ABI.  They
+// have the shape of the reference's installable-tool example
+// (tests/ExternalTool/tool.{hpp,cpp}: a Tool subclass plus a C-linkage
+// create_object(name, once) factory), so a step loop can name the library
+// in a <Tool type="installable" path="libaqua_cuda_tool.so"> element:
 //
-// setup() reads the case's Variables and Definitions from the registry and
-// creates the device context; every execution uploads the particle
-// Variables, runs one step, checks it and downloads the Variables and the
-// scalars t, dt, iter.
+//   - a tool named "link-list..." replaces the link-list tool
+//     (LinkList.cpp:326-494): r_in in; icell, id_sorted, id_unsorted, ihoc,
+//     n_cells, r_min, r_max out;
+//   - any other name replaces the tools from "predictor" to "iter += 1"
+//     (basic.xml:132-171 with the midpoint, domain, cfd, deltaSPH, BIe and
+//     variableTimeStep presets): setup() reads the case's Variables and
+//     Definitions and creates the device context; every execution uploads
+//     the particle Variables, runs one step, checks it and downloads the
+//     Variables and the scalars t, dt, iter.
 #include <cstring>
 #include <string>
 #include <vector>
@@ -191,6 +194,129 @@ class AquaCudaStep : public Tool
     size_t _vs = 4;
 };
 
+// The link-list tool alone, on the registry's host Variables: r_in (vec*),
+// N, h, support and dims in; icell, id_sorted, id_unsorted, ihoc (unsigned
+// int*, ihoc sized for the cell capacity), n_cells (4 unsigned ints), r_min
+// and r_max (vec) out.
+class AquaCudaLinkList : public Tool
+{
+  public:
+    AquaCudaLinkList(const std::string tool_name, bool once)
+      : Tool(tool_name, once)
+    {
+    }
+    ~AquaCudaLinkList() override { release(); }
+
+    void setup() override
+    {
+        setDependencies({ "N", "dims", "h", "support", "r_in" },
+                        { "icell", "id_sorted", "id_unsorted", "ihoc",
+                          "n_cells", "r_min", "r_max" });
+        Tool::setup();
+        release();
+        const int32_t dims = scalar<int32_t>(variables(), "dims");
+        _n = scalar<uint32_t>(variables(), "N");
+        _vs = dims == 3 ? 4 : 2;
+        Variable* ih = variables().get("ihoc");
+        _cap = (uint32_t)(ih->bytes / sizeof(uint32_t));
+        // the link-list needs only h, support and the dimension; the other
+        // parameters are placeholders the context validates
+        static const float one = 1.f;
+        aqua_params p;
+        std::memset(&p, 0, sizeof(p));
+        p.dims = dims;
+        p.n_sets = 1;
+        p.h = scalar<float>(variables(), "h");
+        p.support = scalar<float>(variables(), "support");
+        p.H = p.h;
+        p.CONW = p.CONF = p.SUPPORT = p.DIMS = 1.f;
+        p.refd = p.visc_dyn = p.delta = &one;
+        p.iter_midpoint_max = 1;
+        for (int k = 0; k < 4; k++) {
+            p.domain_min[k] = -1.f;
+            p.domain_max[k] = 1.f;
+        }
+        check("aqua_create", aqua_create(&p, _n, _cap, &_ctx));
+        const size_t nb = (size_t)_n * sizeof(uint32_t);
+        check("aqua_malloc", aqua_malloc(&_r, (size_t)_n * _vs * sizeof(float)));
+        check("aqua_malloc", aqua_malloc(&_icell, nb));
+        check("aqua_malloc", aqua_malloc(&_ids, nb));
+        check("aqua_malloc", aqua_malloc(&_idu, nb));
+        check("aqua_malloc", aqua_malloc(&_ihoc, (size_t)_cap * sizeof(uint32_t)));
+    }
+
+  protected:
+    void _execute() override
+    {
+        Variables& v = variables();
+        const size_t nb = (size_t)_n * sizeof(uint32_t);
+        check("aqua_memcpy",
+              aqua_memcpy(_r, array(v, "r_in", (size_t)_n * _vs * sizeof(float)),
+                          (size_t)_n * _vs * sizeof(float), AQUA_COPY_H2D));
+        uint32_t n_cells[4];
+        float rmin[4], rmax[4];
+        check("aqua_linklist",
+              aqua_linklist(_ctx, static_cast<const float*>(_r), _n,
+                            static_cast<uint32_t*>(_icell),
+                            static_cast<uint32_t*>(_ids),
+                            static_cast<uint32_t*>(_idu),
+                            static_cast<uint32_t*>(_ihoc), _cap, n_cells, rmin,
+                            rmax, nullptr));
+        check("aqua_memcpy", aqua_memcpy(array(v, "icell", nb), _icell, nb,
+                                         AQUA_COPY_D2H));
+        check("aqua_memcpy", aqua_memcpy(array(v, "id_sorted", nb), _ids, nb,
+                                         AQUA_COPY_D2H));
+        check("aqua_memcpy", aqua_memcpy(array(v, "id_unsorted", nb), _idu, nb,
+                                         AQUA_COPY_D2H));
+        const size_t hb = (size_t)n_cells[3] * sizeof(uint32_t);
+        check("aqua_memcpy", aqua_memcpy(array(v, "ihoc", hb), _ihoc, hb,
+                                         AQUA_COPY_D2H));
+        std::memcpy(array(v, "n_cells", sizeof(n_cells)), n_cells, sizeof(n_cells));
+        std::memcpy(array(v, "r_min", _vs * sizeof(float)), rmin, _vs * sizeof(float));
+        std::memcpy(array(v, "r_max", _vs * sizeof(float)), rmax, _vs * sizeof(float));
+    }
+
+  private:
+    template<typename T>
+    static T scalar(Variables& v, const std::string& name)
+    {
+        T x;
+        std::memcpy(&x, array(v, name, sizeof(T)), sizeof(T));
+        return x;
+    }
+    static void* array(Variables& v, const std::string& name, size_t bytes)
+    {
+        Variable* var = v.get(name);
+        if (!var->data || var->bytes < bytes)
+            throw std::runtime_error("Variable \"" + name + "\" holds " +
+                                     std::to_string(var->bytes) + " bytes, " +
+                                     std::to_string(bytes) + " needed");
+        return var->data;
+    }
+    static void check(const char* what, aqua_status s)
+    {
+        if (s != AQUA_OK)
+            throw std::runtime_error(status_text(what, s));
+    }
+    void release()
+    {
+        for (void** p : { &_r, &_icell, &_ids, &_idu, &_ihoc }) {
+            aqua_free(*p);
+            *p = nullptr;
+        }
+        if (_ctx) {
+            aqua_destroy(_ctx);
+            _ctx = nullptr;
+        }
+    }
+
+    aqua_ctx* _ctx = nullptr;
+    void *_r = nullptr, *_icell = nullptr, *_ids = nullptr, *_idu = nullptr,
+         *_ihoc = nullptr;
+    uint32_t _n = 0, _cap = 0;
+    size_t _vs = 4;
+};
+
 }  // namespace aqua_host
 
 // The factory the reference's CalcServer resolves with dlsym
@@ -198,5 +324,7 @@ class AquaCudaStep : public Tool
 extern "C" aqua_host::Tool*
 create_object(const std::string name, bool once)
 {
+    if (name.compare(0, 9, "link-list") == 0)
+        return new aqua_host::AquaCudaLinkList(name, once);
     return new aqua_host::AquaCudaStep(name, once);
 }

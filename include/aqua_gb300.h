@@ -32,6 +32,7 @@
 #ifndef AQUA_GB300_H
 #define AQUA_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -178,6 +179,16 @@ typedef struct aqua_ctx aqua_ctx;
 
 /* Library version string */
 const char* aqua_version(void);
+
+/* Device memory for bindings that have no CUDA runtime of their own (ctypes,
+ * JNI, a host tool): allocate, free, and copy with a wait.  kind:
+ * AQUA_COPY_H2D, AQUA_COPY_D2H or AQUA_COPY_D2D. */
+#define AQUA_COPY_H2D 0
+#define AQUA_COPY_D2H 1
+#define AQUA_COPY_D2D 2
+aqua_status aqua_malloc(void** ptr, size_t bytes);
+aqua_status aqua_free(void* ptr);
+aqua_status aqua_memcpy(void* dst, const void* src, size_t bytes, int kind);
 
 /* Creates a context for cases of up to `capacity` particles on the current
  * device.  `ihoc_capacity` bounds n_cells.w (0 = derive it from the domain

@@ -74,3 +74,38 @@ def test_once_tool_runs_once(rt):
     rt.run(3)
     assert int(arrays["iter"][0]) == c.iter + 1
     rt.clear()
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_link_list_tool_matches_reference_kernels(rt, dims):
+    """The link-list tool alone, on the reference's LinkList test input
+    (tests/{2D,3D}/LinkList), gives the link-list the reference's own kernels
+    give, bit for bit."""
+    g = np.load(os.path.join(GOLD, f"linklist_{dims}d.npz"))
+    n = len(g["r"])
+    vs = 4 if dims == 3 else 2
+    cap = 1 << 16
+    rt.clear()
+    sv = rt.set_variable
+    sv("N", "unsigned int", np.uint32(n).reshape(1))
+    sv("dims", "int", np.int32(dims).reshape(1))
+    sv("h", "float", np.float32([g["h"]]))
+    sv("support", "float", np.float32([g["support"]]))
+    sv("r_in", "vec*", np.ascontiguousarray(g["r"], np.float32))
+    out = {k: sv(k, "unsigned int*", np.zeros(n, np.uint32))
+           for k in ("icell", "id_sorted", "id_unsorted")}
+    out["ihoc"] = sv("ihoc", "unsigned int*", np.zeros(cap, np.uint32))
+    out["n_cells"] = sv("n_cells", "uivec4", np.zeros(4, np.uint32))
+    out["r_min"] = sv("r_min", "vec", np.zeros(vs, np.float32))
+    out["r_max"] = sv("r_max", "vec", np.zeros(vs, np.float32))
+    rt.add_installable("link-list")
+    rt.setup()
+    rt.run(1)
+    nw = int(out["n_cells"][3])
+    assert same(out["n_cells"], g["n_cells"])
+    assert same(out["r_min"][:dims], g["r_min"][:dims])
+    assert same(out["r_max"][:dims], g["r_max"][:dims])
+    for k in ("icell", "id_sorted", "id_unsorted"):
+        assert same(out[k], g[k]), k
+    assert same(out["ihoc"][:nw], g["ihoc"])
+    rt.clear()

@@ -99,3 +99,15 @@ def test_setup_rejects_a_short_variable(rt):
     with pytest.raises(host.HostError, match="\"g\" holds 4 bytes"):
         rt.setup()
     rt.clear()
+
+
+def test_link_list_tool_is_built_by_name(rt):
+    """create_object("link-list...") builds the link-list tool: it needs r_in
+    and its outputs, not the step's Variables."""
+    from aquagpusph_gb300 import host
+    rt.clear()
+    rt.add_installable("link-list")
+    assert rt.tool_count() == 1
+    with pytest.raises(host.HostError, match="unregistered Variable"):
+        rt.setup()
+    rt.clear()
