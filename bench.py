@@ -58,39 +58,24 @@ def workload(name):
     if name == "c2":
         b = cases.sloshing_batch_2d()
         BATCH["c2"] = b
-        return b.case, ("batched 2-D sloshing: 64 closed tanks 0.9x0.5 m, fill "
-                        "U[0.1,0.4] m (numpy default_rng(2026)), dx=0.004 m, "
-                        "h=0.008 m, c0=25, BIe walls, roll about the bottom "
-                        "centre with amplitude U[2,8] deg and period U[1.2,2] s, "
-                        f"one probe per tank: N={b.case.N}")
-    if name == "c4":
+        c = b.case
+    elif name == "c4":
         c = cases.dam_break_3d(dx=0.003)
-        c.dt = c.params.dt_fixed
-        return c, ("3-D dam break at dx=0.003 m, h=0.006 m (SPHERIC test-2 tank "
-                   "3.22x1.0x1.0 m, block 1.228x1.0x0.55 m), BIe walls on 5 "
-                   f"faces, 4 probes: N={c.N}")
-    if name == "c1s":
+    elif name == "c1s":
         c, _ = cpu_sample("c1")
-        return c, ("3-D dam break slab at dx=0.005 m, h=0.01 m (tank "
-                   f"0.8x0.2x0.6 m, block 0.4x0.2x0.55 m): N={c.N}")
-    if name == "c1m":
+    elif name == "c1m":
         # profiling size: same lattice, state (~0.8 GB) well above the L2
         c = cases.dam_break_3d(tank=(1.6, 0.5, 0.6), block=(0.8, 0.5, 0.55),
                                probes_z=(0.02, 0.06))
-        c.dt = c.params.dt_fixed
-        return c, ("3-D dam break at dx=0.005 m, h=0.01 m (tank 1.6x0.5x0.6 m, "
-                   f"block 0.8x0.5x0.55 m): N={c.N}")
-    if name == "c0":
+    elif name == "c0":
         c = cases.dam_break_2d()
-        desc = ("2-D dam break, tank 3.22x1.8 m, column 1.2x0.6 m, dx=0.01 m, "
-                f"h=0.02 m, c0=45, BIe walls, 1 probe: N={c.N}")
     else:
+        name = "c1"
         c = cases.dam_break_3d()
-        desc = ("3-D dam break, SPHERIC test-2 tank 3.22x1.0x1.0 m, block "
-                "1.228x1.0x0.55 m, dx=0.005 m, h=0.01 m, c0=40, BIe walls on "
-                f"5 faces, 4 probes: N={c.N}")
-    c.dt = c.params.dt_fixed
-    return c, desc
+    if name != "c2":
+        c.dt = c.params.dt_fixed
+    assert c.N == WORKLOADS[name][1], (name, c.N)
+    return c, workload_desc(name)
 
 
 def cpu_sample(name):
@@ -264,18 +249,33 @@ def run_reference(args):
     return 0
 
 
+# every workload's description and particle count: both arms of the bench
+# report the same config
+WORKLOADS = {
+    "c1": ("3-D dam break, SPHERIC test-2 tank 3.22x1.0x1.0 m, block "
+           "1.228x1.0x0.55 m, dx=0.005 m, h=0.01 m, c0=40, BIe walls on 5 "
+           "faces, 4 probes", 5878404),
+    "c2": ("batched 2-D sloshing: 64 closed tanks 0.9x0.5 m, fill U[0.1,0.4] m "
+           "(numpy default_rng(2026)), dx=0.004 m, h=0.008 m, c0=25, BIe walls, "
+           "roll about the bottom centre with amplitude U[2,8] deg and period "
+           "U[1.2,2] s, one probe per tank", 935414),
+    "c4": ("3-D dam break at dx=0.003 m, h=0.006 m (SPHERIC test-2 tank "
+           "3.22x1.0x1.0 m, block 1.228x1.0x0.55 m), BIe walls on 5 faces, "
+           "4 probes", 26217760),
+    "c1m": ("3-D dam break at dx=0.005 m, h=0.01 m (tank 1.6x0.5x0.6 m, block "
+            "0.8x0.5x0.55 m)", 1892802),
+    "c1s": ("3-D dam break slab at dx=0.005 m, h=0.01 m (tank 0.8x0.2x0.6 m, "
+            "block 0.4x0.2x0.55 m)", 406402),
+    "c0": ("2-D dam break, tank 3.22x1.8 m, column 1.2x0.6 m, dx=0.01 m, "
+           "h=0.02 m, c0=45, BIe walls, 1 probe", 8205),
+}
+
+
 def workload_desc(name):
-    if name in ("c2", "c3"):
-        return "batched 2-D sloshing, 64 tanks, dx=0.004 m (N=935,414)"
-    if name == "c4":
-        return "3-D dam break, SPHERIC test-2 geometry at dx=0.003 m (~25M particles)"
-    if name == "c1m":
-        return "3-D dam break, 1.6x0.5x0.6 m tank, dx=0.005 m"
-    if name == "c1s":
-        return "3-D dam break slab, dx=0.005 m"
-    if name == "c0":
-        return "2-D dam break (N=8,205)"
-    return "3-D dam break, SPHERIC test-2 geometry, dx=0.005 m (N=5,878,404)"
+    if name == "c3":
+        return workload_desc("c2") + "; one step = one proposal of k=8 plain steps"
+    d, n = WORKLOADS.get(name, WORKLOADS["c1"])
+    return f"{d}: N={n}"
 
 
 def run_ours(args):
@@ -647,8 +647,9 @@ def run_learned(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * dt_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 network (f32 accumulate), f32 state", "data": "synthetic",
-        "config": {"workload": workload_desc("c2") + "; one step = one proposal "
-                   f"of k={K} plain steps", "training": {
+        "config": {"workload": workload_desc("c3") if K == 8 else
+                   workload_desc("c2") + f"; one step = one proposal of k={K} "
+                   "plain steps", "training": {
                        "tanks": "32 sloshing tanks, seed 1234 (config-2 distribution)",
                        "pairs": args.train_pairs, "iterations": args.train_iters,
                        "cases_per_step": 16, "train_s": train_s,
