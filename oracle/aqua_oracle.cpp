@@ -3,7 +3,7 @@
  * canonical preset stack basic + midpoint + domain + cfd + deltaSPH + BIe +
  * variableTimeStep, Morris viscosity, Wendland kernel).
  *
- * TEST INFRASTRUCTURE ONLY.  It is the checker for the CUDA library and the
+ * TEST INFRASTRUCTURE ONLY.  It is the oracle of the CUDA library and the
  * timed CPU baseline of bench.py; the product never links it.  It is pinned
  * by tests/test_oracle_pin.py against (a) the reference's own kernel sources
  * compiled on the host (oracle/refshim/ref_kernels.cpp, bit-exact on whole

@@ -1,5 +1,5 @@
 /*
- * Host-side data contract shared by the two CPU checkers of this repository.
+ * Host-side data contract shared by the two CPU oracles of this repository.
  * TEST INFRASTRUCTURE ONLY (the product never includes or links it):
  *
  *   liboracle.so          -- oracle/aqua_oracle.cpp: an independent C++

@@ -1,4 +1,4 @@
-"""ctypes front end of the CPU checkers (TEST INFRASTRUCTURE ONLY).
+"""ctypes front end of the CPU oracles (TEST INFRASTRUCTURE ONLY).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
 ``bench.py`` import this module, and only to check or to time against; the
@@ -165,7 +165,7 @@ class OracleState:
 
 
 class Oracle:
-    """One of the checker libraries."""
+    """One of the oracle libraries."""
 
     def __init__(self, path):
         self.path = path

@@ -1,7 +1,7 @@
 /*
  * OpenCL-C -> C++ shim for compiling the reference's own kernel sources on
  * the host CPU.  TEST INFRASTRUCTURE ONLY: this header is used exclusively by
- * oracle/refshim/ref_kernels.cpp to build the checker library under
+ * oracle/refshim/ref_kernels.cpp to build the reference-kernel oracle under
  * oracle/_ref/; nothing in the product links it.
  *
  * It shadows the reference's `resources/Scripts/types/types.h` (the kernel
