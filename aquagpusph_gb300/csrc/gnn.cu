@@ -1022,6 +1022,92 @@ k_probe_pressure(uint32_t n_cases, const uint32_t* __restrict__ off,
     }
 }
 
+// Several probes of one large case: fixed grid, each thread sums its
+// grid-stride particles for every probe, the blocks reduce in a fixed tree
+// and a last kernel adds the blocks' partials in block order, so the result
+// does not depend on scheduling.
+constexpr int kProbeBlocks = AQUA_GNN_PROBE_BLOCKS;
+constexpr int kProbeThreads = 256;
+
+template<int D>
+__global__ void __launch_bounds__(kProbeThreads)
+k_probes_partial(uint32_t n, const float* __restrict__ r,
+                 const float* __restrict__ rho, const float* __restrict__ m,
+                 const int32_t* __restrict__ imove, uint32_t n_probes,
+                 const uint32_t* __restrict__ probe, float H, float CONW,
+                 float SUPPORT, float cs, float p0, float refd, float* partial)
+{
+    constexpr int VS = D == 3 ? 4 : 2;
+    constexpr uint32_t P = AQUA_GNN_MAX_PROBES;
+    __shared__ float red[2][kProbeThreads];
+    float pr[P][3];
+    float sp[P], sw[P];
+    for (uint32_t k = 0; k < P; k++) {
+        sp[k] = sw[k] = 0.f;
+        for (int d = 0; d < 3; d++)
+            pr[k][d] = (k < n_probes && d < D) ? r[(size_t)probe[k] * VS + d] : 0.f;
+    }
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n;
+         j += gridDim.x * blockDim.x) {
+        if (imove[j] != 1)
+            continue;
+        float rj[3];
+        for (int d = 0; d < D; d++)
+            rj[d] = r[(size_t)j * VS + d];
+        const float w0 = CONW * m[j] / rho[j];
+        const float pj = p0 + cs * cs * (rho[j] - refd);
+        for (uint32_t k = 0; k < P; k++) {
+            if (k >= n_probes)
+                break;
+            float rr = 0.f;
+            for (int d = 0; d < D; d++) {
+                const float dd = rj[d] - pr[k][d];
+                rr += dd * dd;
+            }
+            const float q = sqrtf(rr) / H;
+            if (q >= SUPPORT)
+                continue;
+            const float a = 2.f - q;
+            const float wq = (D == 3 ? 0.08203125f : 0.109375f) * 0.318309886f *
+                             (1.f + 2.f * q) * a * a * a * a;
+            const float w = wq * w0;
+            sw[k] += w;
+            sp[k] += pj * w;
+        }
+    }
+    for (uint32_t k = 0; k < n_probes && k < P; k++) {
+        red[0][threadIdx.x] = sp[k];
+        red[1][threadIdx.x] = sw[k];
+        __syncthreads();
+        for (int o = kProbeThreads / 2; o > 0; o >>= 1) {
+            if ((int)threadIdx.x < o) {
+                red[0][threadIdx.x] += red[0][threadIdx.x + o];
+                red[1][threadIdx.x] += red[1][threadIdx.x + o];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            partial[(size_t)(2 * k) * kProbeBlocks + blockIdx.x] = red[0][0];
+            partial[(size_t)(2 * k + 1) * kProbeBlocks + blockIdx.x] = red[1][0];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void
+k_probes_final(uint32_t n_probes, const float* __restrict__ partial, float* out)
+{
+    const uint32_t k = threadIdx.x;
+    if (k >= n_probes)
+        return;
+    float sp = 0.f, sw = 0.f;
+    for (int b = 0; b < kProbeBlocks; b++) {
+        sp += partial[(size_t)(2 * k) * kProbeBlocks + b];
+        sw += partial[(size_t)(2 * k + 1) * kProbeBlocks + b];
+    }
+    out[k] = sp / (sw < 1.0e-6f ? 1.f : sw);
+}
+
 __global__ void
 k_case_max_diff(uint32_t n_cases, const uint32_t* __restrict__ off,
                 const float* __restrict__ a, const float* __restrict__ b,
@@ -1492,6 +1578,31 @@ aqua_gnn_case_max_diff(uint32_t n_cases, const uint32_t* off, const float* a,
     k_case_max_diff<<<blocks_for((uint64_t)n_cases * 32, 128), 128, 0,
                       (cudaStream_t)stream>>>(n_cases, off, a, b, imove, scale,
                                               out);
+    return last_error();
+}
+
+aqua_status
+aqua_gnn_probes_pressure(uint32_t n, int32_t dims, const float* r,
+                         const float* rho, const float* m,
+                         const int32_t* imove, uint32_t n_probes,
+                         const uint32_t* probe, const float* k, float* scratch,
+                         float* out, void* stream)
+{
+    if ((dims != 2 && dims != 3) || !r || !rho || !m || !imove || !probe ||
+        !k || !scratch || !out || n_probes > AQUA_GNN_MAX_PROBES)
+        return AQUA_ERR_INVALID;
+    if (n_probes == 0)
+        return AQUA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (dims == 3)
+        k_probes_partial<3><<<kProbeBlocks, kProbeThreads, 0, s>>>(
+            n, r, rho, m, imove, n_probes, probe, k[0], k[1], k[2], k[3], k[4],
+            k[5], scratch);
+    else
+        k_probes_partial<2><<<kProbeBlocks, kProbeThreads, 0, s>>>(
+            n, r, rho, m, imove, n_probes, probe, k[0], k[1], k[2], k[3], k[4],
+            k[5], scratch);
+    k_probes_final<<<1, 32, 0, s>>>(n_probes, scratch, out);
     return last_error();
 }
 

@@ -221,6 +221,17 @@ k_linear_fwd_tc(uint32_t M, uint32_t K, const uint16_t* __restrict__ X,
 // the values the unfused layers store to and reload from global memory, so
 // the result is bit-identical to three aqua_gnn_linear_fwd_tc calls.  Only
 // the BF16 output of layer 3 is written.
+//
+// With SUM the layer-3 output never leaves the chip either: it is summed
+// into the receivers (aqua_gnn_segment_sum fused in).  Each CTA owns a
+// contiguous range of receivers (about E / grid edges) and walks its edges
+// in 128-edge tiles, in order.  The layer-3 tile is staged in shared memory
+// (row-major, 16-byte groups XOR-swizzled by row), the receivers' runs of
+// rows are summed by the warps (run k by warp k mod 4, lanes over column
+// pairs), and a receiver whose edges continue in the next tile carries its
+// partial sums there.  Every receiver's sum is thus the same sequence of
+// FP32 additions, in edge order from zero, as aqua_gnn_segment_sum's: the
+// output is bit-identical to the unfused kernels'.
 
 __device__ __forceinline__ void
 cp_async_16z(void* dst, const void* src, bool valid)
@@ -231,7 +242,27 @@ cp_async_16z(void* dst, const void* src, bool valid)
                  : "memory");
 }
 
-template<int K1, bool PAIR>
+// bytes of the operand buffer: the layer-1 input or a 128 x 64 bf16 tile
+template<int K1>
+__host__ __device__ constexpr uint32_t
+edge_operand_bytes()
+{
+    constexpr uint32_t a0 = ((128u * K1 * 2u + 1023u) / 1024u) * 1024u;
+    constexpr uint32_t a1 = 128u * 64u * 2u;
+    return a0 > a1 ? a0 : a1;
+}
+
+// the receiver-sum bookkeeping of a SUM CTA (shared memory after the
+// operand buffer)
+struct SumShared {
+    uint32_t recv[kTcRows];   // receiver of each row of the tile (~0: none)
+    uint32_t start[4];        // rows that start a receiver's run, per warp
+    float carry[2][64];       // partial sums carried into the next tile
+    uint32_t carry_node[2];   // their receiver (~0: none)
+    uint32_t nodes[2];        // this CTA's receivers [nodes[0], nodes[1])
+};
+
+template<int K1, bool PAIR, bool SUM>
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
               const uint32_t* __restrict__ recv, const uint32_t* __restrict__ send,
@@ -240,7 +271,9 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
               const uint16_t* __restrict__ W1, const float* __restrict__ b1,
               const uint16_t* __restrict__ W2, const float* __restrict__ b2,
               const uint16_t* __restrict__ W3, const float* __restrict__ b3,
-              int act1, int act2, int act3, uint16_t* Y, uint32_t ldy, int* err)
+              int act1, int act2, int act3, uint16_t* Y, uint32_t ldy, int* err,
+              uint32_t n_nodes, const uint32_t* __restrict__ off, float scale,
+              uint32_t col)
 {
     constexpr uint32_t kW1 = ((64u * K1 * 2u + 1023u) / 1024u) * 1024u;
     constexpr uint32_t kW = 64u * 64u * 2u;            // W2, W3
@@ -251,9 +284,11 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     uint8_t* sW2 = sW1 + kW1;
     uint8_t* sW3 = sW2 + kW;
     // one operand buffer: the layer-1 input (128 x K1), then, once layer 1's
-    // MMAs have completed, the 128 x 64 activations of layers 1 and 2
+    // MMAs have completed, the 128 x 64 activations of layers 1 and 2 (and,
+    // with SUM, the layer-3 output tile)
     uint8_t* sA0 = sW3 + kW;
     uint8_t* sA1 = sA0;
+    SumShared* ss = reinterpret_cast<SumShared*>(sA0 + edge_operand_bytes<K1>());
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     stage(sW1, W1, K1, 64, 64, K1);
@@ -344,10 +379,51 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         *reinterpret_cast<uint4*>(sA1 + ((r / 8) * 8 + g) * 128 + (r % 8) * 16) = val;
     };
 
-    const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
-    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
-        const uint32_t e = tile * kTcRows + r;
-        const bool valid = e < E;
+    // the edges of this CTA: every tile (grid-stride), or, with SUM, the
+    // edges of its receivers
+    uint32_t e_begin = 0, e_end = E;
+    if constexpr (SUM) {
+        if (threadIdx.x == 0) {
+            // first node s in [0, n_nodes] with off[s] >= v
+            auto lower = [&](uint64_t v) -> uint32_t {
+                uint32_t lo = 0, hi = n_nodes;
+                while (lo < hi) {
+                    const uint32_t mid = lo + (hi - lo) / 2;
+                    if ((uint64_t)off[mid] < v)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                return lo;
+            };
+            const uint64_t G = gridDim.x;
+            ss->nodes[0] = blockIdx.x == 0 ? 0u : lower((uint64_t)blockIdx.x * E / G);
+            ss->nodes[1] = blockIdx.x + 1 == gridDim.x
+                               ? n_nodes
+                               : lower((uint64_t)(blockIdx.x + 1) * E / G);
+            ss->carry_node[0] = ss->carry_node[1] = 0xffffffffu;
+        }
+        __syncthreads();
+        const uint32_t n_lo = ss->nodes[0], n_hi = ss->nodes[1];
+        // receivers without edges: a zero sum
+        for (uint32_t s = n_lo + threadIdx.x; s < n_hi; s += kTcThreads)
+            if (off[s] == off[s + 1]) {
+                uint4* dst = reinterpret_cast<uint4*>(Y + (size_t)s * ldy + col);
+                for (int g = 0; g < 8; g++)
+                    dst[g] = make_uint4(0u, 0u, 0u, 0u);
+            }
+        e_begin = off[n_lo];
+        e_end = off[n_hi];
+    }
+    const uint32_t tiles = SUM ? (e_end - e_begin + kTcRows - 1) / kTcRows
+                               : (E + kTcRows - 1) / kTcRows;
+    for (uint32_t tile = SUM ? 0u : blockIdx.x; tile < tiles && !failed;
+         tile += SUM ? 1u : gridDim.x) {
+        const uint32_t eb = e_begin + tile * kTcRows;
+        const uint32_t e = eb + r;
+        const bool valid = e < e_end;
+        if constexpr (SUM)
+            ss->recv[r] = valid ? recv[e] : 0xffffffffu;
         // layer-1 input rows, gathered asynchronously into sA0
         constexpr uint32_t kg = K1 / 8;
         uint8_t* row0 = sA0 + (r / 8) * kg * 128 + (r % 8) * 16;
@@ -381,10 +457,72 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
             failed = true;
             break;
         }
-        epilogue(b3, act3, [&](int g, uint4 val) {
-            if (valid)
-                *reinterpret_cast<uint4*>(Y + (size_t)e * ldy + g * 8) = val;
-        });
+        if constexpr (!SUM) {
+            epilogue(b3, act3, [&](int g, uint4 val) {
+                if (valid)
+                    *reinterpret_cast<uint4*>(Y + (size_t)e * ldy + g * 8) = val;
+            });
+        } else {
+            // layer-3 tile into shared memory: row r at r * 128 bytes, its
+            // 16-byte group g at position g ^ (r % 8)
+            epilogue(b3, act3, [&](int g, uint4 val) {
+                *reinterpret_cast<uint4*>(sA1 + r * 128u + ((g ^ (r & 7u)) * 16u)) = val;
+            });
+            const uint32_t nvalid = min((uint32_t)kTcRows, e_end - eb);
+            const bool st = r < nvalid && (r == 0 || ss->recv[r] != ss->recv[r - 1]);
+            const uint32_t bal = __ballot_sync(0xffffffffu, st);
+            if (lane == 0)
+                ss->start[warp] = bal;
+            __syncthreads();
+            const uint32_t par = tile & 1u;
+            uint32_t ord = 0;
+            for (uint32_t wq = 0; wq < 4; wq++) {
+                uint32_t m = ss->start[wq];
+                while (m) {
+                    const uint32_t a = wq * 32u + (uint32_t)(__ffs(m) - 1);
+                    m &= m - 1;
+                    if ((ord++ & 3u) != warp)
+                        continue;
+                    // the run ends at the next start or at the last row
+                    uint32_t b = nvalid;
+                    if (m) {
+                        b = wq * 32u + (uint32_t)(__ffs(m) - 1);
+                    } else {
+                        for (uint32_t w2 = wq + 1; w2 < 4; w2++) {
+                            const uint32_t m2 = ss->start[w2];
+                            if (m2) {
+                                b = w2 * 32u + (uint32_t)(__ffs(m2) - 1);
+                                break;
+                            }
+                        }
+                    }
+                    const uint32_t node = ss->recv[a];
+                    float a0 = 0.f, a1 = 0.f;
+                    if (a == 0 && ss->carry_node[par] == node) {
+                        a0 = ss->carry[par][2 * lane];
+                        a1 = ss->carry[par][2 * lane + 1];
+                    }
+                    for (uint32_t k = a; k < b; k++) {
+                        const uint32_t v = *reinterpret_cast<const uint32_t*>(
+                            sA1 + k * 128u + (((lane >> 2) ^ (k & 7u)) * 16u) +
+                            (lane & 3u) * 4u);
+                        a0 += __uint_as_float(v << 16);
+                        a1 += __uint_as_float(v & 0xffff0000u);
+                    }
+                    if (off[node + 1] <= eb + nvalid) {
+                        *reinterpret_cast<uint32_t*>(Y + (size_t)node * ldy + col +
+                                                     2 * lane) =
+                            pack2(a0 * scale, a1 * scale);
+                    } else {
+                        // the last run: its receiver continues in the next tile
+                        ss->carry[par ^ 1u][2 * lane] = a0;
+                        ss->carry[par ^ 1u][2 * lane + 1] = a1;
+                        if (lane == 0)
+                            ss->carry_node[par ^ 1u] = node;
+                    }
+                }
+            }
+        }
         // the next tile's copies and MMAs reuse sA0, sA1 and the accumulator
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();
@@ -397,14 +535,67 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     }
 }
 
-template<int K1, bool PAIR>
+template<int K1, bool SUM>
 constexpr size_t
 edge_mlp_smem()
 {
-    constexpr size_t a0 = ((128u * K1 * 2u + 1023u) / 1024u) * 1024u;
-    constexpr size_t a1 = 128u * 64u * 2u;
     return ((64u * K1 * 2u + 1023u) / 1024u) * 1024u + 2u * 64u * 64u * 2u +
-           (a0 > a1 ? a0 : a1);
+           edge_operand_bytes<K1>() + (SUM ? sizeof(SumShared) : 0u);
+}
+
+}  // namespace
+
+namespace {
+
+// sets the shared-memory limit of the four fused edge-MLP kernels once per
+// device (the limit is a per-device attribute of each kernel)
+aqua_status
+edge_mlp_configure(int& sms)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+            cudaSuccess)
+        return AQUA_ERR_CUDA;
+    static std::atomic<uint64_t> configured{ 0 };
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (!bit || !(configured.load() & bit)) {
+        const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        if (cudaFuncSetAttribute(k_edge_mlp_tc<16, false, false>, a,
+                                 (int)edge_mlp_smem<16, false>()) != cudaSuccess ||
+            cudaFuncSetAttribute(k_edge_mlp_tc<144, true, false>, a,
+                                 (int)edge_mlp_smem<144, false>()) != cudaSuccess ||
+            cudaFuncSetAttribute(k_edge_mlp_tc<16, false, true>, a,
+                                 (int)edge_mlp_smem<16, true>()) != cudaSuccess ||
+            cudaFuncSetAttribute(k_edge_mlp_tc<144, true, true>, a,
+                                 (int)edge_mlp_smem<144, true>()) != cudaSuccess)
+            return AQUA_ERR_CUDA;
+        configured.fetch_or(bit);
+    }
+    return AQUA_OK;
+}
+
+bool
+a16(const void* p)
+{
+    return (reinterpret_cast<uintptr_t>(p) & 15) == 0;
+}
+
+// the arguments both fused forms share
+bool
+edge_mlp_args_ok(uint32_t K1, const uint16_t* X, uint32_t ldx,
+                 const uint32_t* recv, const uint32_t* send, const uint16_t* H,
+                 uint32_t ldh, const uint16_t* Ef, const uint16_t* W1,
+                 const float* b1, const uint16_t* W2, const float* b2,
+                 const uint16_t* W3, const float* b3, const int32_t* err)
+{
+    if (!W1 || !b1 || !W2 || !b2 || !W3 || !b3 || !err || !a16(W1) ||
+        !a16(W2) || !a16(W3))
+        return false;
+    if (X == nullptr)
+        return K1 == 144 && recv && send && H && Ef && ldh >= 64 && ldh % 8 == 0 &&
+               a16(H) && a16(Ef);
+    return K1 == AQUA_GNN_FEATURES && ldx >= K1 && ldx % 8 == 0 && a16(X);
 }
 
 }  // namespace
@@ -418,53 +609,80 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
                      int32_t act1, int32_t act2, int32_t act3, uint16_t* Y,
                      uint32_t ldy, int32_t* err, void* stream)
 {
-    auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
     const bool pair = (X == nullptr);
-    if (!W1 || !b1 || !W2 || !b2 || !W3 || !b3 || !Y || !err || ldy < 64 ||
-        ldy % 8 || !a16(Y) || !a16(W1) || !a16(W2) || !a16(W3))
+    if (!edge_mlp_args_ok(K1, X, ldx, recv, send, H, ldh, Ef, W1, b1, W2, b2,
+                          W3, b3, err) ||
+        !Y || ldy < 64 || ldy % 8 || !a16(Y))
         return AQUA_ERR_INVALID;
-    if (pair) {
-        if (K1 != 144 || !recv || !send || !H || !Ef || ldh < 64 || ldh % 8 ||
-            !a16(H) || !a16(Ef))
-            return AQUA_ERR_INVALID;
-    } else if (K1 != AQUA_GNN_FEATURES || ldx < K1 || ldx % 8 || !a16(X)) {
-        return AQUA_ERR_INVALID;
-    }
     if (E == 0)
         return AQUA_OK;
-    int sms = 0, dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
-            cudaSuccess)
-        return AQUA_ERR_CUDA;
-    // the shared-memory limit is a per-device attribute of each kernel
-    static std::atomic<uint64_t> configured{ 0 };
-    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
-    if (!bit || !(configured.load() & bit)) {
-        if (cudaFuncSetAttribute(k_edge_mlp_tc<16, false>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)edge_mlp_smem<16, false>()) != cudaSuccess ||
-            cudaFuncSetAttribute(k_edge_mlp_tc<144, true>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)edge_mlp_smem<144, true>()) != cudaSuccess)
-            return AQUA_ERR_CUDA;
-        configured.fetch_or(bit);
-    }
+    int sms = 0;
+    const aqua_status st = edge_mlp_configure(sms);
+    if (st != AQUA_OK)
+        return st;
     const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
     cudaStream_t s = (cudaStream_t)stream;
     if (pair) {
         // 72 KB of shared memory: three CTAs per SM (192 of 512 TMEM columns)
         const uint32_t grid = tiles < (uint32_t)sms * 3u ? tiles : (uint32_t)sms * 3u;
-        k_edge_mlp_tc<144, true><<<grid, kTcThreads, edge_mlp_smem<144, true>(), s>>>(
-            E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
-            act1, act2, act3, Y, ldy, err);
+        k_edge_mlp_tc<144, true, false>
+            <<<grid, kTcThreads, edge_mlp_smem<144, false>(), s>>>(
+                E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
+                act1, act2, act3, Y, ldy, err, 0u, nullptr, 0.f, 0u);
     } else {
         // 34 KB: at most six CTAs per SM (384 TMEM columns)
         const uint32_t grid = tiles < (uint32_t)sms * 6u ? tiles : (uint32_t)sms * 6u;
-        k_edge_mlp_tc<16, false><<<grid, kTcThreads, edge_mlp_smem<16, false>(), s>>>(
-            E, X, ldx, nullptr, nullptr, nullptr, 0, nullptr, W1, b1, W2, b2, W3,
-            b3, act1, act2, act3, Y, ldy, err);
+        k_edge_mlp_tc<16, false, false>
+            <<<grid, kTcThreads, edge_mlp_smem<16, false>(), s>>>(
+                E, X, ldx, nullptr, nullptr, nullptr, 0, nullptr, W1, b1, W2,
+                b2, W3, b3, act1, act2, act3, Y, ldy, err, 0u, nullptr, 0.f, 0u);
     }
+    return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
+}
+
+extern "C" aqua_status
+aqua_gnn_edge_mlp_sum_tc(uint32_t n_nodes, uint32_t E, uint32_t K1,
+                         const uint16_t* X, uint32_t ldx,
+                         const uint32_t* offsets, const uint32_t* recv,
+                         const uint32_t* send, const uint16_t* H, uint32_t ldh,
+                         const uint16_t* Ef, const uint16_t* W1,
+                         const float* b1, const uint16_t* W2, const float* b2,
+                         const uint16_t* W3, const float* b3, int32_t act1,
+                         int32_t act2, int32_t act3, float scale,
+                         uint16_t* out, uint32_t ld, uint32_t col,
+                         int32_t* err, void* stream)
+{
+    const bool pair = (X == nullptr);
+    if (!edge_mlp_args_ok(K1, X, ldx, recv, send, H, ldh, Ef, W1, b1, W2, b2,
+                          W3, b3, err) ||
+        !offsets || !recv || !out || !a16(out) || ld % 8 || col % 8 ||
+        col + 64 > ld || E >= 0x80000000u)
+        return AQUA_ERR_INVALID;
+    if (n_nodes == 0)
+        return AQUA_OK;
+    int sms = 0;
+    const aqua_status st = edge_mlp_configure(sms);
+    if (st != AQUA_OK)
+        return st;
+    // each CTA owns the receivers of about E / grid edges; a small graph
+    // gets fewer CTAs (at least one, for the receivers without edges)
+    const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
+    const uint32_t per_sm = pair ? 3u : 6u;
+    uint32_t grid = (uint32_t)sms * per_sm;
+    if (tiles < grid)
+        grid = tiles > 0 ? tiles : 1u;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (pair)
+        k_edge_mlp_tc<144, true, true>
+            <<<grid, kTcThreads, edge_mlp_smem<144, true>(), s>>>(
+                E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
+                act1, act2, act3, out, ld, err, n_nodes, offsets, scale, col);
+    else
+        k_edge_mlp_tc<16, false, true>
+            <<<grid, kTcThreads, edge_mlp_smem<16, true>(), s>>>(
+                E, X, ldx, recv, nullptr, nullptr, 0, nullptr, W1, b1, W2, b2,
+                W3, b3, act1, act2, act3, out, ld, err, n_nodes, offsets, scale,
+                col);
     return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
 }
 

@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import time
 
 import numpy as np
 
@@ -38,12 +39,18 @@ LAYERS = [
     ("n2_0", 64, 144, 1), ("n2_1", 64, 64, 1), ("n2_2", 16, 64, 0),
 ]
 AGG_SCALE = 1.0 / 32.0
+# aqua_gnn_probes_pressure: probes per call and device scratch (floats)
+MAX_PROBES = 8
+PROBE_SCRATCH = 2 * MAX_PROBES * 256
 # 64-wide layers run on tcgen05 (tensor memory) when True, on mma.sync
 # otherwise (the 16-wide output layer always uses mma.sync)
 USE_TCGEN05 = True
 # inference runs each edge MLP as one fused tcgen05 kernel (inputs gathered
 # and activations kept on chip) when True
 FUSE_EDGE_MLP = True
+# ... and sums its output into the receivers on chip as well (no E x 64
+# intermediate) when True
+FUSE_EDGE_SUM = True
 
 _vp = C.c_void_p
 
@@ -69,47 +76,56 @@ def _chk(name, st):
 _u32, _i32, _f32 = C.c_uint32, C.c_int32, C.c_float
 # argument types of every function of include/aqua_learned.h
 SIGNATURES = {
-        "aqua_gnn_cell_keys": [_u32, _i32, _vp, _vp, _vp, _f32, _vp, _vp, _vp, _vp, _vp],
-        "aqua_gnn_cell_ranges": [_u32, _vp, _u32, _vp, _vp, _vp],
-        "aqua_gnn_neighbours": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _f32, _vp, _vp,
-                                _vp, _vp, _vp],
-        "aqua_gnn_bbox": [_u32, _i32, _vp, _vp, _vp, _vp, _vp],
-        "aqua_gnn_exclusive_scan": [_u32, _vp, _vp, _vp, _vp],
-        "aqua_gnn_gather32": [_u32, _vp, _vp, _u32, _u32, _vp, _vp],
-        "aqua_gnn_scatter32": [_u32, _vp, _vp, _u32, _vp, _u32, _vp],
-        "aqua_gnn_node_features": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                                   _vp, _u32, _u32, _vp],
-        "aqua_gnn_edge_features": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                                   _vp, _vp, _vp],
-        "aqua_gnn_linear_fwd": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32, _vp,
-                                _u32, _i32, _vp],
-        "aqua_gnn_linear_fwd_tc": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32,
-                               _vp, _u32, _i32, _vp, _vp],
-        "aqua_gnn_edge_mlp_tc": [_u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32, _vp,
-                                 _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32,
-                                 _vp, _u32, _vp, _vp],
-    "aqua_gnn_linear_dgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _u32, _i32,
-                                  _vp, _u32, _vp],
-        "aqua_gnn_linear_wgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _u32, _vp, _vp, _vp],
-        "aqua_gnn_segment_sum": [_u32, _vp, _vp, _u32, _f32, _vp, _u32, _u32, _vp],
-        "aqua_gnn_segment_bcast": [_u32, _vp, _vp, _u32, _u32, _f32, _vp, _u32, _vp],
-        "aqua_gnn_gather_pair": [_u32, _vp, _vp, _vp, _u32, _vp, _vp, _vp],
-        "aqua_gnn_scatter_pair": [_u32, _u32, _vp, _vp, _vp, _vp, _vp],
-        "aqua_gnn_add_to_bf16": [_u32, _vp, _vp, _u32, _u32, _vp, _u32, _u32, _vp],
-        "aqua_gnn_mse": [_u32, _u32, _vp, _vp, _vp, _f32, _vp, _vp, _vp],
-        "aqua_gnn_adam": [_u32, _vp, _vp, _vp, _vp, _f32, _f32, _f32, _f32, _u32, _vp,
-                          _vp],
-        "aqua_gnn_to_bf16": [_u32, _vp, _vp, _vp],
-        "aqua_gnn_transpose": [_u32, _u32, _vp, _vp, _vp],
-        "aqua_gnn_apply": [_u32, _i32, _vp, _vp, _vp, _vp, _u32, _f32, _f32, _vp, _vp,
-                           _vp, _vp, _vp, _vp, _vp],
-        "aqua_gnn_targets": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                             _vp, _u32, _f32, _f32, _vp, _vp, _vp, _vp],
-        "aqua_gnn_roll": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                          _vp, _vp, _vp, _vp, _vp],
-        "aqua_gnn_probe_pressure": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                                    _vp],
-        "aqua_gnn_case_max_diff": [_u32, _vp, _vp, _vp, _vp, _f32, _vp, _vp],
+    "aqua_gnn_cell_keys": [_u32, _i32, _vp, _vp, _vp, _f32, _vp, _vp, _vp, _vp,
+                           _vp],
+    "aqua_gnn_cell_ranges": [_u32, _vp, _u32, _vp, _vp, _vp],
+    "aqua_gnn_neighbours": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _f32, _vp, _vp,
+                            _vp, _vp, _vp],
+    "aqua_gnn_bbox": [_u32, _i32, _vp, _vp, _vp, _vp, _vp],
+    "aqua_gnn_exclusive_scan": [_u32, _vp, _vp, _vp, _vp],
+    "aqua_gnn_gather32": [_u32, _vp, _vp, _u32, _u32, _vp, _vp],
+    "aqua_gnn_scatter32": [_u32, _vp, _vp, _u32, _vp, _u32, _vp],
+    "aqua_gnn_node_features": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                               _vp, _u32, _u32, _vp],
+    "aqua_gnn_edge_features": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                               _vp, _vp, _vp],
+    "aqua_gnn_linear_fwd": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32,
+                            _vp, _u32, _i32, _vp],
+    "aqua_gnn_linear_fwd_tc": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp,
+                               _u32, _vp, _u32, _i32, _vp, _vp],
+    "aqua_gnn_edge_mlp_tc": [_u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32, _vp,
+                             _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32,
+                             _vp, _u32, _vp, _vp],
+    "aqua_gnn_edge_mlp_sum_tc": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp,
+                                 _vp, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                 _i32, _i32, _i32, _f32, _vp, _u32, _u32, _vp,
+                                 _vp],
+    "aqua_gnn_linear_dgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _u32,
+                              _i32, _vp, _u32, _vp],
+    "aqua_gnn_linear_wgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _u32, _vp, _vp,
+                              _vp],
+    "aqua_gnn_segment_sum": [_u32, _vp, _vp, _u32, _f32, _vp, _u32, _u32, _vp],
+    "aqua_gnn_segment_bcast": [_u32, _vp, _vp, _u32, _u32, _f32, _vp, _u32,
+                               _vp],
+    "aqua_gnn_gather_pair": [_u32, _vp, _vp, _vp, _u32, _vp, _vp, _vp],
+    "aqua_gnn_scatter_pair": [_u32, _u32, _vp, _vp, _vp, _vp, _vp],
+    "aqua_gnn_add_to_bf16": [_u32, _vp, _vp, _u32, _u32, _vp, _u32, _u32, _vp],
+    "aqua_gnn_mse": [_u32, _u32, _vp, _vp, _vp, _f32, _vp, _vp, _vp],
+    "aqua_gnn_adam": [_u32, _vp, _vp, _vp, _vp, _f32, _f32, _f32, _f32, _u32,
+                      _vp, _vp],
+    "aqua_gnn_to_bf16": [_u32, _vp, _vp, _vp],
+    "aqua_gnn_transpose": [_u32, _u32, _vp, _vp, _vp],
+    "aqua_gnn_apply": [_u32, _i32, _vp, _vp, _vp, _vp, _u32, _f32, _f32, _vp,
+                       _vp, _vp, _vp, _vp, _vp, _vp],
+    "aqua_gnn_targets": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                         _vp, _u32, _f32, _f32, _vp, _vp, _vp, _vp],
+    "aqua_gnn_roll": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                      _vp, _vp, _vp, _vp, _vp],
+    "aqua_gnn_probe_pressure": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                _vp],
+    "aqua_gnn_probes_pressure": [_u32, _i32, _vp, _vp, _vp, _vp, _u32, _vp, _vp,
+                                 _vp, _vp, _vp],
+    "aqua_gnn_case_max_diff": [_u32, _vp, _vp, _vp, _vp, _f32, _vp, _vp],
 }
 
 
@@ -345,13 +361,15 @@ class Network:
     """Forward (and, with ``train``, backward) of the model on one graph."""
 
     def __init__(self, model: Model, graph: Graph, inputs: Inputs, stream=None,
-                 tcgen05=None, fused=None):
+                 tcgen05=None, fused=None, fused_sum=None):
         torch = _torch()
         self.model, self.g, self.x = model, graph, inputs
         self.s = _vp(stream or 0)
         self.stream = stream
         self.tc = USE_TCGEN05 if tcgen05 is None else bool(tcgen05)
         self.fused = self.tc and (FUSE_EDGE_MLP if fused is None else bool(fused))
+        self.fused_sum = self.fused and (FUSE_EDGE_SUM if fused_sum is None
+                                         else bool(fused_sum))
         self.err = torch.zeros(1, dtype=torch.int32, device=graph.rs.device)
 
     def _buf(self, shape, dtype):
@@ -415,6 +433,24 @@ class Network:
             _p(y), 64, _p(self.err), self.s))
         return y
 
+    def _edge_mlp_sum(self, prefix, out, ld, X=None, ldx=0, H=None, ldh=0,
+                      Ef=None):
+        """The fused edge MLP summed into the receivers: AGG_SCALE times the
+        sum of each node's edge outputs, bf16 at column 0 of ``out`` (rows
+        ``ld`` apart)."""
+        m = self.model
+        names = [f"{prefix}_{k}" for k in range(3)]
+        acts = [m.offs[nm][4] for nm in names]
+        k1 = m.offs[names[0]][3]
+        g = self.g
+        _chk("aqua_gnn_edge_mlp_sum_tc", lib().aqua_gnn_edge_mlp_sum_tc(
+            g.n_nodes, g.n_edges, k1, X or _vp(0), ldx, _p(g.offsets),
+            _p(g.receivers), _p(g.senders) if H is not None else _vp(0),
+            H or _vp(0), ldh, Ef or _vp(0),
+            m.W(names[0]), m.b(names[0]), m.W(names[1]), m.b(names[1]),
+            m.W(names[2]), m.b(names[2]), acts[0], acts[1], acts[2],
+            AGG_SCALE, _p(out), ld, 0, _p(self.err), self.s))
+
     def forward(self, train=False):
         torch = _torch()
         L = lib()
@@ -428,14 +464,19 @@ class Network:
             _p(x.imove), _p(x.normal), _p(m.scales), _p(E0), s))
         c["E0"] = E0
         fused = self.fused and not train
-        if fused:
-            A, Z = [self._edge_mlp_fused("e1", E, X=_p(E0), ldx=FEAT)], []
-        else:
-            A, Z = self._mlp("e1", _p(E0), FEAT, E, train)
-        c["e1"] = (A, Z)
+        summed = self.fused_sum and not train
         n1_in = self._buf((n, 80), torch.bfloat16)
-        _chk("aqua_gnn_segment_sum", L.aqua_gnn_segment_sum(
-            n, _p(g.offsets), _p(A[-1]), 64, AGG_SCALE, _p(n1_in), 80, 0, s))
+        if summed:
+            self._edge_mlp_sum("e1", n1_in, 80, X=_p(E0), ldx=FEAT)
+        else:
+            if fused:
+                A, Z = [self._edge_mlp_fused("e1", E, X=_p(E0), ldx=FEAT)], []
+            else:
+                A, Z = self._mlp("e1", _p(E0), FEAT, E, train)
+            c["e1"] = (A, Z)
+            _chk("aqua_gnn_segment_sum", L.aqua_gnn_segment_sum(
+                n, _p(g.offsets), _p(A[-1]), 64, AGG_SCALE, _p(n1_in), 80, 0, s))
+            del A, Z
         _chk("aqua_gnn_node_features", L.aqua_gnn_node_features(
             n, dims, _p(x.u), _p(x.rho), _p(x.dudt), _p(x.drhodt), _p(x.imove),
             _p(x.normal), _p(m.scales), _p(n1_in), 80, 64, s))
@@ -444,18 +485,25 @@ class Network:
         H = _vp(n2_in.data_ptr() + 2 * 64)
         A, Z = self._mlp("n1", _p(n1_in), 80, n, train, out=H, ldo=144)
         c["n1"] = (A, Z)
-        if fused:
-            # the pair inputs are gathered on chip: X2 is never built
-            A, Z = [self._edge_mlp_fused("e2", E, H=H, ldh=144, Ef=_p(E0))], []
+        if summed:
+            self._edge_mlp_sum("e2", n2_in, 144, H=H, ldh=144, Ef=_p(E0))
         else:
-            X2 = self._buf((max(E, 1), 144), torch.bfloat16)
-            _chk("aqua_gnn_gather_pair", L.aqua_gnn_gather_pair(
-                E, _p(g.receivers), _p(g.senders), H, 144, _p(E0), _p(X2), s))
-            c["X2"] = X2
-            A, Z = self._mlp("e2", _p(X2), 144, E, train)
-        c["e2"] = (A, Z)
-        _chk("aqua_gnn_segment_sum", L.aqua_gnn_segment_sum(
-            n, _p(g.offsets), _p(A[-1]), 64, AGG_SCALE, _p(n2_in), 144, 0, s))
+            if fused:
+                # the pair inputs are gathered on chip: X2 is never built
+                A, Z = [self._edge_mlp_fused("e2", E, H=H, ldh=144,
+                                             Ef=_p(E0))], []
+            else:
+                X2 = self._buf((max(E, 1), 144), torch.bfloat16)
+                _chk("aqua_gnn_gather_pair", L.aqua_gnn_gather_pair(
+                    E, _p(g.receivers), _p(g.senders), H, 144, _p(E0), _p(X2),
+                    s))
+                c["X2"] = X2
+                A, Z = self._mlp("e2", _p(X2), 144, E, train)
+            c["e2"] = (A, Z)
+            _chk("aqua_gnn_segment_sum", L.aqua_gnn_segment_sum(
+                n, _p(g.offsets), _p(A[-1]), 64, AGG_SCALE, _p(n2_in), 144, 0,
+                s))
+            del A, Z
         _chk("aqua_gnn_node_features", L.aqua_gnn_node_features(
             n, dims, _p(x.u), _p(x.rho), _p(x.dudt), _p(x.drhodt), _p(x.imove),
             _p(x.normal), _p(m.scales), _p(n2_in), 144, 128, s))
@@ -673,14 +721,16 @@ class Trainer:
     """Adam on the masked MSE of the normalised residual targets."""
 
     def __init__(self, model, solver, batch, k, lr=1e-3, cases_per_step=16,
-                 seed=0):
+                 seed=0, radius=None):
         self.model, self.sv, self.batch, self.k = model, solver, batch, k
         self.lr = lr
         self.cases = cases_per_step
         self.rng = np.random.default_rng(seed)
         self.cid = case_ids(batch)
         self.offsets = np.asarray(batch.offsets, np.int64)
-        self.radius = float(batch.case.params.support * batch.case.params.h)
+        p = batch.case.params
+        # graph radius: the kernel support 2h unless given
+        self.radius = float(radius) if radius else float(p.support * p.h)
         self.history = []
 
     def _slice(self, snap, a, b):
@@ -914,3 +964,150 @@ class ProposalRunner:
         _lib.check("aqua_set_cases", solver.lib.aqua_set_cases(
             solver.ctx, n, offs.ctypes.data_as(_lib._U), arr, _vp(0)))
         solver.n_cases = n
+
+
+class FieldProposalRunner:
+    """Advances one large case by learned k-step proposals, each judged by
+    the plain step over the whole field.
+
+    Each ``advance()``: the network proposes the state k plain steps ahead
+    (graph radius ``radius``, default 0.9 h: with h = 2 dx, the 26 nearest
+    lattice neighbours); the plain step re-runs the same k
+    steps from the same state in a second solver context; the proposal is
+    compared with it at every probe of the case (Shepard-interpolated
+    pressure, ``aqua_gnn_probes_pressure``) and, for density, on a random
+    subsample of ``rho_sample`` of the fluid particles drawn anew each time.
+    If a probe departs by more than ``tol`` of max(|p_plain|, p_floor), or
+    the subsample's density by more than ``tol`` of refd, the whole field
+    takes the plain state (rollback); otherwise the proposal stands."""
+
+    def __init__(self, solver, case, model, k=8, radius=None, rho_sample=0.1,
+                 tol=0.02, p_floor=None, seed=0, fast=True):
+        from .solver import Solver
+        torch = _torch()
+        self.sv, self.model, self.k = solver, model, k
+        self.dims = case.dims
+        p = case.params
+        self.params = p
+        self.radius = float(radius) if radius else 0.9 * float(p.h)
+        self.tol = tol
+        self.rng = np.random.default_rng(seed)
+        self.refd = float(p.refd[0])
+        g = abs(float(np.asarray(p.g)[1 if self.dims == 2 else 2]))
+        self.p_floor = p_floor if p_floor is not None else self.refd * g * 4 * p.h
+        self.n = case.N
+        self.cid = torch.zeros(case.N, dtype=torch.int32, device="cuda")
+        self.consts = (C.c_float * 6)(p.H, p.CONW, p.SUPPORT, p.cs, p.p0,
+                                      self.refd)
+        # particles in original order (= id): the probes and the fluid
+        imove = np.asarray(case.imove)
+        probes = np.nonzero(imove == 0)[0].astype(np.int32)
+        if len(probes) > MAX_PROBES:
+            raise ValueError(f"at most {MAX_PROBES} probes")
+        self.probes = torch.from_numpy(probes).cuda()
+        self.fluid = np.nonzero(imove == 1)[0].astype(np.int32)
+        self.n_sub = max(1, int(round(rho_sample * len(self.fluid))))
+        self.scratch = torch.empty(PROBE_SCRATCH, dtype=torch.float32,
+                                   device="cuda")
+        self.judge = Solver(p, capacity=case.N)
+        self.judge.set_precision(fast)
+        self.stats = {"proposals": 0, "rolled_back": 0, "p_err": [],
+                      "rho_err": [], "n_edges": 0, "phase_s": {}}
+
+    def _phase(self, name, t0):
+        torch = _torch()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ph = self.stats["phase_s"]
+        ph[name] = ph.get(name, 0.0) + (t1 - t0)
+        return t1
+
+    def probe_pressures(self, snap):
+        """Pressure at every probe of a snapshot (device, one per probe)."""
+        torch = _torch()
+        out = torch.empty(len(self.probes), dtype=torch.float32, device="cuda")
+        _chk("aqua_gnn_probes_pressure", lib().aqua_gnn_probes_pressure(
+            snap.n, self.dims, _p(snap["r"]), _p(snap["rho"]), _p(snap["m"]),
+            _p(snap["imove"]), len(self.probes), _p(self.probes), self.consts,
+            _p(self.scratch), _p(out), _vp(0)))
+        return out
+
+    def _rho_err(self, a, b):
+        """max |rho_a - rho_b| / refd over a fresh random subsample of the
+        fluid particles."""
+        torch = _torch()
+        L = lib()
+        sub = np.sort(self.rng.choice(self.fluid, self.n_sub, replace=False))
+        idx = torch.from_numpy(sub.astype(np.int32)).cuda()
+        m = len(sub)
+        ra = torch.empty(m, dtype=torch.float32, device="cuda")
+        rb = torch.empty_like(ra)
+        im = torch.ones(m, dtype=torch.int32, device="cuda")
+        for src, dst in ((a, ra), (b, rb)):
+            _chk("aqua_gnn_gather32", L.aqua_gnn_gather32(
+                m, _p(idx), _p(src), 1, 1, _p(dst), _vp(0)))
+        off = torch.tensor([0, m], dtype=torch.int32, device="cuda")
+        er = torch.empty(1, dtype=torch.float32, device="cuda")
+        _chk("aqua_gnn_case_max_diff", L.aqua_gnn_case_max_diff(
+            1, _p(off), _p(ra), _p(rb), _p(im), 1.0 / self.refd, _p(er),
+            _vp(0)))
+        return float(er.item())
+
+    def advance(self):
+        """One proposal of k steps (synchronises)."""
+        torch = _torch()
+        L = lib()
+        dims, k = self.dims, self.k
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc = self.sv.scalars()
+        dt = torch.tensor([sc["dt"]], dtype=torch.float32, device="cuda")
+        s0 = Snapshot.capture(self.sv, dims)
+        n = s0.n
+        t0 = self._phase("snapshot", t0)
+        # ---- proposal
+        g = Graph(self.sv, dims, s0["r"], s0["imove"], self.cid, n, self.radius)
+        self.stats["n_edges"] = g.n_edges
+        t0 = self._phase("graph", t0)
+        x = Inputs(g, s0["r"], s0["u"], s0["rho"], s0["dudt"], s0["drhodt"],
+                   s0["imove"], s0["normal"])
+        out = Network(self.model, g, x).forward(train=False)
+        s1 = s0.clone()
+        su, srho = self.model.out_scale
+        _chk("aqua_gnn_apply", L.aqua_gnn_apply(
+            g.n_nodes, dims, _p(g.perm), _p(out), _p(self.cid), _p(dt), k, su,
+            srho, _p(s1["r"]), _p(s1["u"]), _p(s1["rho"]), _p(s0["dudt"]),
+            _p(s0["drhodt"]), _p(s0["imove"]), _vp(0)))
+        del x, out, g
+        t0 = self._phase("network", t0)
+        # ---- plain judge over the whole field, from the same state
+        self.judge.set_state_raw(n, s0.ptrs(), False, sc["t"], sc["dt"],
+                                 sc["iter"])
+        self.judge.step(k, graph=True)
+        self.judge.check()
+        t0 = self._phase("judge", t0)
+        plain = Snapshot.capture(self.judge, dims)
+        pp = self.probe_pressures(s1).cpu().numpy()
+        pj = self.probe_pressures(plain).cpu().numpy()
+        p_err = np.abs(pp - pj) / np.maximum(np.abs(pj), self.p_floor)
+        rho_err = self._rho_err(s1["rho"], plain["rho"])
+        bad = bool((p_err > self.tol).any() or rho_err > self.tol)
+        t0 = self._phase("compare", t0)
+        # ---- rollback (the plain field) or the proposal becomes resident
+        if bad:
+            js = self.judge.scalars()
+            self.sv.set_state_raw(n, plain.ptrs(), False, js["t"], js["dt"],
+                                  js["iter"])
+        else:
+            self.sv.set_state_raw(n, s1.ptrs(), False, sc["t"] + k * sc["dt"],
+                                  sc["dt"], sc["iter"] + k)
+        self._phase("set_state", t0)
+        st = self.stats
+        st["proposals"] += 1
+        st["rolled_back"] += int(bad)
+        st["p_err"].extend(p_err.tolist())
+        st["rho_err"].append(rho_err)
+        return p_err, rho_err, bad
+
+    def close(self):
+        self.judge.close()

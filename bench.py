@@ -82,6 +82,8 @@ def cpu_sample(name):
     """A bounded sample of the workload for the CPU runs: the same lattice,
     smoothing length, constants and wall treatment on a smaller tank."""
     from aquagpusph_gb300 import case as cases
+    if name == "c5":
+        name = "c4"
     if name in ("c2", "c3"):
         b = cases.sloshing_batch_2d()
         return b, (f"the whole batch (64 tanks, N={b.case.N}), each tank "
@@ -274,6 +276,11 @@ WORKLOADS = {
 def workload_desc(name):
     if name == "c3":
         return workload_desc("c2") + "; one step = one proposal of k=8 plain steps"
+    if name == "c5":
+        return (workload_desc("c4") + "; one step = one learned proposal of k=8 "
+                "plain steps (graph radius 0.9h: 26 lattice neighbours), "
+                "judged every proposal by the plain step over the whole field "
+                "(4 probes, density on a 10% fluid subsample)")
     d, n = WORKLOADS.get(name, WORKLOADS["c1"])
     return f"{d}: N={n}"
 
@@ -686,6 +693,167 @@ def run_learned(args):
     return 0
 
 
+def run_learned_3d(args):
+    """Learned k = 8 proposals on the 26M-particle 3-D dam break, each judged
+    by the plain step over the whole field; the network is first trained on
+    plain trajectories of a small dam break with the same dx, h and walls."""
+    import torch
+    from aquagpusph_gb300 import case as cases
+    from aquagpusph_gb300 import learned as Lm
+    from aquagpusph_gb300.solver import Solver
+    torch.cuda.set_device(0)
+    K = 8
+    t0 = time.perf_counter()
+    small = cases.dam_break_3d(dx=0.003, tank=(0.48, 0.12, 0.36),
+                               block=(0.24, 0.12, 0.33), probes_z=(0.02,))
+    small.dt = small.params.dt_fixed
+    tb = cases.pack([small])
+    radius = 0.9 * small.params.h
+    pairs, dts = Lm.collect_pairs(tb, K, n_pairs=args.train_pairs, gap=100,
+                                  warm=200)
+    model = Lm.Model(3, seed=0)
+    Lm.fit_scales(model, pairs, dts, K, small.params, Lm.case_ids(tb))
+    sv_t = Solver(small.params, capacity=small.N)
+    tr = Lm.Trainer(model, sv_t, tb, K, lr=1e-3, cases_per_step=1,
+                    radius=radius)
+    held = list(range(len(pairs) - 4, len(pairs)))
+
+    def held_loss(m):
+        tr.model = m
+        v = [float(tr.batch_loss(pairs[i], dts[i], 0, 1, train=False)[1].item())
+             for i in held]
+        tr.model = model
+        return float(np.mean(v))
+    zero = Lm.Model(3, seed=0)
+    zero.flat.zero_()
+    zero._refresh()
+    zero.scales.copy_(model.scales)
+    zero.out_scale = model.out_scale
+    loss_zero = held_loss(zero)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.train_iters):
+        tr.step(pairs[:-4], dts[:-4])
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    loss_trained = held_loss(model)
+    sv_t.close()
+    del pairs, dts, tr
+    prep_s = time.perf_counter() - t0
+
+    c, _ = workload("c4")
+    sv = Solver(c.params, capacity=c.N)
+    sv.set_precision(args.precision == "fast")
+    sv.set_case(c)
+    sv.step(args.eval_warm, graph=True)
+    sv.check()
+    run = Lm.FieldProposalRunner(sv, c, model, k=K, radius=radius,
+                                 rho_sample=0.1, tol=0.02,
+                                 fast=args.precision == "fast")
+    for _ in range(args.warmup):
+        run.advance()
+    st = run.stats
+    st.update(proposals=0, rolled_back=0, p_err=[], rho_err=[], phase_s={})
+    clocks = ClockSampler(0)
+    clocks.start()
+    calls0 = Lm.CALLS[0]
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    for _ in range(args.steps):
+        run.advance()
+    torch.cuda.synchronize()
+    dt_s = time.perf_counter() - t2
+    clk = clocks.stop()
+    calls = Lm.CALLS[0] - calls0
+    judge_launches = args.steps * K * run.judge.launches_per_step()
+    value = c.N * K * args.steps / dt_s
+    # the plain step on the same case, same number of particle-steps
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sv.step(K * args.steps, graph=True)
+    e1.record()
+    e1.synchronize()
+    sv.check()
+    plain_ms = e0.elapsed_time(e1)
+    plain_value = c.N * K * args.steps / (plain_ms * 1e-3)
+    # the network forward alone on the current state, CUDA events
+    s0 = Lm.Snapshot.capture(sv, 3)
+    g = Lm.Graph(sv, 3, s0["r"], s0["imove"], run.cid, s0.n, radius)
+    x = Lm.Inputs(g, s0["r"], s0["u"], s0["rho"], s0["dudt"], s0["drhodt"],
+                  s0["imove"], s0["normal"])
+    net = Lm.Network(model, g, x)
+    net.forward()
+    e0.record()
+    net.forward()
+    e1.record()
+    e1.synchronize()
+    fwd_ms = e0.elapsed_time(e1)
+    flops = 0
+    for name, n, kk, act in Lm.LAYERS:
+        rows = g.n_edges if name[0] == "e" else g.n_nodes
+        flops += 2 * rows * n * kk
+    n_edges = g.n_edges
+    del net, x, g, s0
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("bf16_tflops") or 1900.0
+    steps = args.steps
+    line = {
+        "metric": "particle-steps/s (learned k=8 proposal judged by the plain "
+                  "step over the whole field, 1 GB300)",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt_s / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 network (f32 accumulate), f32 state", "data": "synthetic",
+        "config": {"workload": workload_desc("c5"), "training": {
+                       "case": "3-D dam break slab at dx=0.003 m, h=0.006 m: "
+                               "tank 0.48x0.12x0.36 m, block 0.24x0.12x0.33 m, "
+                               f"N={small.N}",
+                       "pairs": args.train_pairs, "iterations": args.train_iters,
+                       "train_s": train_s, "prep_s": prep_s},
+                   "judge": "plain k steps over the whole field every proposal; "
+                            "rollback of the whole field at > 2% probe-pressure "
+                            "error (of max(|p|, rho g 4h)) at any of the 4 "
+                            "probes or > 2% density error (of refd) on a 10% "
+                            "fluid subsample"},
+        "plain_value": plain_value, "learned_over_plain": value / plain_value,
+        "heldout_mse": {"trained": loss_trained,
+                        "extrapolation_only": loss_zero},
+        "judge_stats": {"proposals": st["proposals"],
+                        "rolled_back": st["rolled_back"],
+                        "p_err_median": float(np.median(st["p_err"])),
+                        "p_err_max": float(np.max(st["p_err"])),
+                        "rho_err_median": float(np.median(st["rho_err"])),
+                        "rho_err_max": float(np.max(st["rho_err"]))},
+        "phase_ms_per_proposal": {k: 1e3 * v / steps
+                                  for k, v in st["phase_s"].items()},
+        "graph_edges": n_edges,
+        "gpu_launches": calls + judge_launches,
+        "gpu_launches_note": "library entry points called (each launches at "
+                             "least one kernel) plus the judge's plain-step "
+                             "kernels",
+        "roofline": {"bound": "tensor", "kernel": "network forward (fused "
+                     "tcgen05 edge MLPs with on-chip receiver sums, node "
+                     "layers, graph gathers)",
+                     "achieved": flops / (fwd_ms * 1e-3) / 1e12,
+                     "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / (fwd_ms * 1e-3) / 1e12 / peak,
+                     "peak_source": "measured" if peaks.get("bf16_tflops") else "fallback",
+                     "flops_per_forward": flops, "forward_ms": fwd_ms,
+                     "traffic": None},
+        "clocks": clk, "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+    run.close()
+    sv.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -693,10 +861,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c1",
-                    choices=["c1", "c0", "c1s", "c1m", "c2", "c3", "c4"])
+                    choices=["c1", "c0", "c1s", "c1m", "c2", "c3", "c4",
+                             "c5"])
     ap.add_argument("--train-pairs", type=int, default=24)
     ap.add_argument("--train-iters", type=int, default=300)
-    ap.add_argument("--eval-warm", type=int, default=3000)
+    ap.add_argument("--eval-warm", type=int, default=None,
+                    help="plain steps before the proposals (3000 for c3, 40 for c5)")
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--precision", default="fast", choices=["exact", "fast"])
     ap.add_argument("--no-tune", action="store_true")
@@ -708,8 +878,12 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.eval_warm is None:
+        args.eval_warm = 40 if args.workload == "c5" else 3000
     if args.workload == "c3":
         return run_learned(args)
+    if args.workload == "c5":
+        return run_learned_3d(args)
     return run_ours(args)
 
 

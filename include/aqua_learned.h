@@ -141,6 +141,25 @@ aqua_status aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X,
                                  int32_t act1, int32_t act2, int32_t act3,
                                  uint16_t* Y, uint32_t ldy, int32_t* err,
                                  void* stream);
+/* The same fused edge MLP followed by aqua_gnn_segment_sum, with the edge
+ * outputs kept on chip: out[s] (64 bf16 at column col of rows ld apart) =
+ * scale * sum of the layer-3 rows of node s's edges (receiver-major,
+ * offsets[0..n_nodes]; recv is required in both input forms).  Each receiver
+ * is summed in edge order by one CTA, so the result is bit-identical to
+ * aqua_gnn_edge_mlp_tc + aqua_gnn_segment_sum, without the E x 64 bf16
+ * intermediate.  E < 2^31; a time-out of the bounded waits sets *err. */
+aqua_status aqua_gnn_edge_mlp_sum_tc(uint32_t n_nodes, uint32_t E, uint32_t K1,
+                                     const uint16_t* X, uint32_t ldx,
+                                     const uint32_t* offsets,
+                                     const uint32_t* recv, const uint32_t* send,
+                                     const uint16_t* H, uint32_t ldh,
+                                     const uint16_t* Ef, const uint16_t* W1,
+                                     const float* b1, const uint16_t* W2,
+                                     const float* b2, const uint16_t* W3,
+                                     const float* b3, int32_t act1,
+                                     int32_t act2, int32_t act3, float scale,
+                                     uint16_t* out, uint32_t ld, uint32_t col,
+                                     int32_t* err, void* stream);
 /* dX = dY W (M x K, bf16 at ldx) where dY: M x N bf16 (ldy), Wt: K x N.
  * With Zprev (M x K f32, ldzp) and act_prev = AQUA_ACT_SILU the result is
  * multiplied by silu'(Zprev) (the gradient of the previous layer's
@@ -264,6 +283,21 @@ aqua_status aqua_gnn_probe_pressure(uint32_t n_cases, int32_t dims,
                                     const float* rho, const float* m,
                                     const int32_t* imove, const float* consts,
                                     float* out, void* stream);
+/* Pressure at several probes of one case: for each probe k (the particle
+ * probe[k] of the arrays, at most AQUA_GNN_MAX_PROBES), the same Shepard-
+ * normalised interpolation as aqua_gnn_probe_pressure over the fluid
+ * particles of [0, n).  The sums are reduced in a fixed order (a fixed grid
+ * of AQUA_GNN_PROBE_BLOCKS blocks, then the blocks in order): the result is
+ * deterministic.  scratch: AQUA_GNN_PROBE_SCRATCH floats of device memory;
+ * consts (host memory) as for aqua_gnn_probe_pressure. */
+#define AQUA_GNN_MAX_PROBES 8
+#define AQUA_GNN_PROBE_BLOCKS 256
+#define AQUA_GNN_PROBE_SCRATCH (2 * AQUA_GNN_MAX_PROBES * AQUA_GNN_PROBE_BLOCKS)
+aqua_status aqua_gnn_probes_pressure(uint32_t n, int32_t dims, const float* r,
+                                     const float* rho, const float* m,
+                                     const int32_t* imove, uint32_t n_probes,
+                                     const uint32_t* probe, const float* consts,
+                                     float* scratch, float* out, void* stream);
 /* out[c] = max over fluid particles i of case c of |a_i - b_i| * scale */
 aqua_status aqua_gnn_case_max_diff(uint32_t n_cases, const uint32_t* offsets,
                                    const float* a, const float* b,

@@ -219,8 +219,9 @@ def test_proposal_judge_and_rollback(torch):
 
 
 def test_fused_edge_mlps_equal_the_layer_by_layer_forward(torch):
-    """Inference with each edge MLP as one fused tcgen05 kernel gives the
-    layer-by-layer tcgen05 forward bit for bit."""
+    """Inference with each edge MLP as one fused tcgen05 kernel, with or
+    without the receiver sums fused in, gives the layer-by-layer tcgen05
+    forward bit for bit."""
     from aquagpusph_gb300 import learned as Lm
     b = small_batch(3)
     sv, g, x, host = network_inputs(torch, b)
@@ -229,8 +230,11 @@ def test_fused_edge_mlps_equal_the_layer_by_layer_forward(torch):
     model.scales.copy_(torch.tensor((float(b.case.params.h), 0.05, 0.5, 0.5,
                                      5.0, 998.0)))
     outs = []
-    for fused in (False, True):
-        net = Lm.Network(model, g, x, tcgen05=True, fused=fused)
+    for fused, summed in ((False, False), (True, False), (True, True)):
+        net = Lm.Network(model, g, x, tcgen05=True, fused=fused,
+                         fused_sum=summed)
         outs.append(net.forward(train=False).clone())
     assert torch.equal(outs[0], outs[1])
+    # the edge outputs summed into the receivers on chip: the same bits
+    assert torch.equal(outs[0], outs[2])
     sv.close()

@@ -150,3 +150,100 @@ def test_fused_edge_mlp_rejects_bad_arguments(torch):
                                   *args) == -1
     assert L.aqua_gnn_edge_mlp_tc(8, 144, None, 0, None, None, None, 144, None,
                                   *args) == -1
+
+
+def csr_graph(rng, n, mean_deg, n_big=0, big=300):
+    """Receiver-major edges: random degrees (about 10% zero), n_big nodes
+    of degree `big` (runs across several 128-edge tiles), random senders."""
+    deg = rng.integers(0, 2 * mean_deg + 1, n)
+    deg[rng.random(n) < 0.1] = 0
+    if n_big:
+        deg[rng.choice(n, n_big, replace=False)] = big
+    off = np.concatenate([[0], np.cumsum(deg)]).astype(np.uint32)
+    E = int(off[-1])
+    recv = np.repeat(np.arange(n, dtype=np.uint32), deg)
+    send = rng.integers(0, max(n, 1), E).astype(np.uint32)
+    return off, recv, send, E
+
+
+def dev_u32(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)
+                            if len(a) else np.zeros(1, np.int32)).cuda()
+
+
+GRAPHS = [(3, 2, 0, 0), (40, 8, 1, 300), (2500, 40, 5, 700), (25000, 40, 0, 0),
+          (1, 0, 1, 1000), (50, 0, 0, 0)]
+
+
+@pytest.mark.parametrize("pair", [False, True])
+@pytest.mark.parametrize("n,deg,n_big,big", GRAPHS)
+def test_fused_edge_mlp_sum_equals_mlp_then_segment_sum(torch, pair, n, deg,
+                                                        n_big, big):
+    """The edge MLP with the receiver sums fused in gives aqua_gnn_edge_mlp_tc
+    followed by aqua_gnn_segment_sum bit for bit: receivers without edges,
+    receivers whose edges span several tiles (and CTAs' ranges), a graph
+    without edges; the columns of the output rows outside the 64 written
+    stay untouched."""
+    from aquagpusph_gb300 import learned as Lm
+    L = Lm.lib()
+    rng = np.random.default_rng(n * 31 + deg + big + int(pair))
+    off, recv, send, E = csr_graph(rng, n, deg, n_big, big)
+    offd, recvd, sendd = (dev_u32(torch, a) for a in (off, recv, send))
+    Ef = torch.from_numpy(G.bf16(rng.normal(0, 1, (max(E, 1), 16))
+                                 .astype(np.float32))).cuda().to(torch.bfloat16)
+    node = torch.from_numpy(G.bf16(rng.normal(0, 1, (n, 144)).astype(np.float32))
+                            ).cuda().to(torch.bfloat16)
+    H = Lm._vp(node.data_ptr() + 2 * 64)
+    K1 = 144 if pair else 16
+    Ws, bs = weights(torch, rng, K1)
+    acts = (1, 1, 0)
+    wargs = [Lm._p(Ws[0]), Lm._p(bs[0]), Lm._p(Ws[1]), Lm._p(bs[1]),
+             Lm._p(Ws[2]), Lm._p(bs[2]), *acts]
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    Y = torch.empty((max(E, 1), 64), dtype=torch.bfloat16, device="cuda")
+    if pair:
+        inputs = [None, 0, Lm._p(recvd), Lm._p(sendd), H, 144, Lm._p(Ef)]
+    else:
+        inputs = [Lm._p(Ef), 16, None, None, None, 0, None]
+    assert L.aqua_gnn_edge_mlp_tc(E, K1, *inputs, *wargs, Lm._p(Y), 64,
+                                  Lm._p(err), None) == 0
+    ld = 80
+    ref = torch.full((n, ld), 7.0, dtype=torch.bfloat16, device="cuda")
+    assert L.aqua_gnn_segment_sum(n, Lm._p(offd), Lm._p(Y), 64, Lm.AGG_SCALE,
+                                  Lm._p(ref), ld, 8, None) == 0
+    out = torch.full((n, ld), 7.0, dtype=torch.bfloat16, device="cuda")
+    assert L.aqua_gnn_edge_mlp_sum_tc(n, E, K1, inputs[0], inputs[1],
+                                      Lm._p(offd), Lm._p(recvd),
+                                      *inputs[3:], *wargs, Lm.AGG_SCALE,
+                                      Lm._p(out), ld, 8, Lm._p(err), None) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert torch.equal(out.view(torch.int16), ref.view(torch.int16))
+    assert bool((out[:, :8].float() == 7.0).all())
+    assert bool((out[:, 72:].float() == 7.0).all())
+
+
+def test_fused_edge_mlp_sum_rejects_bad_arguments(torch):
+    from aquagpusph_gb300 import learned as Lm
+    L = Lm.lib()
+    W = torch.zeros((64, 144), dtype=torch.bfloat16, device="cuda")
+    b = torch.zeros(64, dtype=torch.float32, device="cuda")
+    X = torch.zeros((8, 16), dtype=torch.bfloat16, device="cuda")
+    out = torch.empty((4, 80), dtype=torch.bfloat16, device="cuda")
+    off = torch.zeros(5, dtype=torch.int32, device="cuda")
+    recv = torch.zeros(8, dtype=torch.int32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    w = [Lm._p(W), Lm._p(b)] * 3 + [1, 1, 0, 0.5]
+    ok = [4, 8, 16, Lm._p(X), 16, Lm._p(off), Lm._p(recv), None, None, 0, None,
+          *w, Lm._p(out), 80, 0, Lm._p(err), None]
+    bad = []
+    for i, v in ((5, None), (6, None), (len(ok) - 5, None)):   # offsets, recv, out
+        a = list(ok)
+        a[i] = v
+        bad.append(a)
+    for i, v in ((len(ok) - 3, 3), (len(ok) - 3, 24), (len(ok) - 4, 68)):
+        a = list(ok)                                         # col, ld
+        a[i] = v
+        bad.append(a)
+    for a in bad:
+        assert L.aqua_gnn_edge_mlp_sum_tc(*a) == -1
