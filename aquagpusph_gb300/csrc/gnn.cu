@@ -1108,6 +1108,43 @@ k_probes_final(uint32_t n_probes, const float* __restrict__ partial, float* out)
     out[k] = sp / (sw < 1.0e-6f ? 1.f : sw);
 }
 
+// 32-bit integer hash (the "lowbias32" mixer: xor-shift / multiply rounds)
+__device__ __forceinline__ uint32_t
+mix32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// max |a_i - b_i| * scale over the fluid particles whose hash of (i, seed)
+// falls below `below` (a Bernoulli subsample of fraction below / 2^32); a
+// non-finite difference counts as infinite.  The maximum of non-negative
+// floats is taken on their bit patterns with atomicMax: order-independent.
+__global__ void
+k_sample_max_diff(uint32_t n, const float* __restrict__ a,
+                  const float* __restrict__ b, const int32_t* __restrict__ imove,
+                  uint32_t seed, uint32_t below, float scale, int* out)
+{
+    float mx = 0.f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        if (imove[i] != 1 || mix32(i ^ mix32(seed)) >= below)
+            continue;
+        float d = fabsf(a[i] - b[i]) * scale;
+        if (!(d <= 3.0e38f))
+            d = INFINITY;
+        mx = fmaxf(mx, d);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > 0.f)
+        atomicMax(out, __float_as_int(mx));
+}
+
 __global__ void
 k_case_max_diff(uint32_t n_cases, const uint32_t* __restrict__ off,
                 const float* __restrict__ a, const float* __restrict__ b,
@@ -1603,6 +1640,25 @@ aqua_gnn_probes_pressure(uint32_t n, int32_t dims, const float* r,
             n, r, rho, m, imove, n_probes, probe, k[0], k[1], k[2], k[3], k[4],
             k[5], scratch);
     k_probes_final<<<1, 32, 0, s>>>(n_probes, scratch, out);
+    return last_error();
+}
+
+aqua_status
+aqua_gnn_sample_max_diff(uint32_t n, const float* a, const float* b,
+                         const int32_t* imove, uint32_t seed, float fraction,
+                         float scale, float* out, void* stream)
+{
+    if (!a || !b || !imove || !out || !(fraction >= 0.f && fraction <= 1.f))
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaMemsetAsync(out, 0, sizeof(float), s) != cudaSuccess)
+        return AQUA_ERR_CUDA;
+    if (n == 0)
+        return AQUA_OK;
+    const double f = (double)fraction * 4294967296.0;
+    const uint32_t below = f >= 4294967295.0 ? 0xffffffffu : (uint32_t)f;
+    k_sample_max_diff<<<blocks_for(n, 256, 152u * 8u), 256, 0, s>>>(
+        n, a, b, imove, seed, below, scale, reinterpret_cast<int*>(out));
     return last_error();
 }
 

@@ -125,6 +125,8 @@ SIGNATURES = {
                                 _vp],
     "aqua_gnn_probes_pressure": [_u32, _i32, _vp, _vp, _vp, _vp, _u32, _vp, _vp,
                                  _vp, _vp, _vp],
+    "aqua_gnn_sample_max_diff": [_u32, _vp, _vp, _vp, _u32, _f32, _f32, _vp,
+                                 _vp],
     "aqua_gnn_case_max_diff": [_u32, _vp, _vp, _vp, _vp, _f32, _vp, _vp],
 }
 
@@ -999,14 +1001,13 @@ class FieldProposalRunner:
         self.cid = torch.zeros(case.N, dtype=torch.int32, device="cuda")
         self.consts = (C.c_float * 6)(p.H, p.CONW, p.SUPPORT, p.cs, p.p0,
                                       self.refd)
-        # particles in original order (= id): the probes and the fluid
+        # particles in original order (= id): the probes
         imove = np.asarray(case.imove)
         probes = np.nonzero(imove == 0)[0].astype(np.int32)
         if len(probes) > MAX_PROBES:
             raise ValueError(f"at most {MAX_PROBES} probes")
         self.probes = torch.from_numpy(probes).cuda()
-        self.fluid = np.nonzero(imove == 1)[0].astype(np.int32)
-        self.n_sub = max(1, int(round(rho_sample * len(self.fluid))))
+        self.rho_sample = float(rho_sample)
         self.scratch = torch.empty(PROBE_SCRATCH, dtype=torch.float32,
                                    device="cuda")
         self.judge = Solver(p, capacity=case.N)
@@ -1032,25 +1033,15 @@ class FieldProposalRunner:
             _p(self.scratch), _p(out), _vp(0)))
         return out
 
-    def _rho_err(self, a, b):
-        """max |rho_a - rho_b| / refd over a fresh random subsample of the
-        fluid particles."""
+    def _rho_err(self, a, b, imove):
+        """max |rho_a - rho_b| / refd over a fresh random subsample (a
+        fraction rho_sample) of the fluid particles."""
         torch = _torch()
-        L = lib()
-        sub = np.sort(self.rng.choice(self.fluid, self.n_sub, replace=False))
-        idx = torch.from_numpy(sub.astype(np.int32)).cuda()
-        m = len(sub)
-        ra = torch.empty(m, dtype=torch.float32, device="cuda")
-        rb = torch.empty_like(ra)
-        im = torch.ones(m, dtype=torch.int32, device="cuda")
-        for src, dst in ((a, ra), (b, rb)):
-            _chk("aqua_gnn_gather32", L.aqua_gnn_gather32(
-                m, _p(idx), _p(src), 1, 1, _p(dst), _vp(0)))
-        off = torch.tensor([0, m], dtype=torch.int32, device="cuda")
         er = torch.empty(1, dtype=torch.float32, device="cuda")
-        _chk("aqua_gnn_case_max_diff", L.aqua_gnn_case_max_diff(
-            1, _p(off), _p(ra), _p(rb), _p(im), 1.0 / self.refd, _p(er),
-            _vp(0)))
+        seed = int(self.rng.integers(0, 2 ** 32))
+        _chk("aqua_gnn_sample_max_diff", lib().aqua_gnn_sample_max_diff(
+            self.n, _p(a), _p(b), _p(imove), seed, self.rho_sample,
+            1.0 / self.refd, _p(er), _vp(0)))
         return float(er.item())
 
     def advance(self):
@@ -1090,7 +1081,7 @@ class FieldProposalRunner:
         pp = self.probe_pressures(s1).cpu().numpy()
         pj = self.probe_pressures(plain).cpu().numpy()
         p_err = np.abs(pp - pj) / np.maximum(np.abs(pj), self.p_floor)
-        rho_err = self._rho_err(s1["rho"], plain["rho"])
+        rho_err = self._rho_err(s1["rho"], plain["rho"], plain["imove"])
         bad = bool((p_err > self.tol).any() or rho_err > self.tol)
         t0 = self._phase("compare", t0)
         # ---- rollback (the plain field) or the proposal becomes resident

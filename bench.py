@@ -716,7 +716,10 @@ def run_learned_3d(args):
     sv_t = Solver(small.params, capacity=small.N)
     tr = Lm.Trainer(model, sv_t, tb, K, lr=1e-3, cases_per_step=1,
                     radius=radius)
-    held = list(range(len(pairs) - 4, len(pairs)))
+    # held-out pairs spread over the trajectory (one in six)
+    held = list(range(3, len(pairs), 6))
+    train_pairs = [q for i, q in enumerate(pairs) if i not in held]
+    train_dts = [q for i, q in enumerate(dts) if i not in held]
 
     def held_loss(m):
         tr.model = m
@@ -733,12 +736,12 @@ def run_learned_3d(args):
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for _ in range(args.train_iters):
-        tr.step(pairs[:-4], dts[:-4])
+        tr.step(train_pairs, train_dts)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t1
     loss_trained = held_loss(model)
     sv_t.close()
-    del pairs, dts, tr
+    del pairs, dts, tr, train_pairs, train_dts
     prep_s = time.perf_counter() - t0
 
     c, _ = workload("c4")
@@ -814,7 +817,8 @@ def run_learned_3d(args):
                        "case": "3-D dam break slab at dx=0.003 m, h=0.006 m: "
                                "tank 0.48x0.12x0.36 m, block 0.24x0.12x0.33 m, "
                                f"N={small.N}",
-                       "pairs": args.train_pairs, "iterations": args.train_iters,
+                       "pairs": args.train_pairs, "held_out": len(held),
+                       "iterations": args.train_iters,
                        "train_s": train_s, "prep_s": prep_s},
                    "judge": "plain k steps over the whole field every proposal; "
                             "rollback of the whole field at > 2% probe-pressure "
@@ -866,7 +870,7 @@ def main():
     ap.add_argument("--train-pairs", type=int, default=24)
     ap.add_argument("--train-iters", type=int, default=300)
     ap.add_argument("--eval-warm", type=int, default=None,
-                    help="plain steps before the proposals (3000 for c3, 40 for c5)")
+                    help="plain steps before the proposals (3000 for c3, 200 for c5)")
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--precision", default="fast", choices=["exact", "fast"])
     ap.add_argument("--no-tune", action="store_true")
@@ -879,7 +883,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.eval_warm is None:
-        args.eval_warm = 40 if args.workload == "c5" else 3000
+        args.eval_warm = 200 if args.workload == "c5" else 3000
     if args.workload == "c3":
         return run_learned(args)
     if args.workload == "c5":

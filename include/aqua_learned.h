@@ -298,6 +298,15 @@ aqua_status aqua_gnn_probes_pressure(uint32_t n, int32_t dims, const float* r,
                                      const int32_t* imove, uint32_t n_probes,
                                      const uint32_t* probe, const float* consts,
                                      float* scratch, float* out, void* stream);
+/* *out (device float) = max of |a_i - b_i| * scale over a random subsample
+ * of the fluid particles (imove == 1) of [0, n): particle i is in it when a
+ * 32-bit hash of (i, seed) falls below fraction * 2^32, so about `fraction`
+ * of them, drawn anew for each seed; a non-finite difference counts as
+ * infinite.  Deterministic for a given seed. */
+aqua_status aqua_gnn_sample_max_diff(uint32_t n, const float* a,
+                                     const float* b, const int32_t* imove,
+                                     uint32_t seed, float fraction, float scale,
+                                     float* out, void* stream);
 /* out[c] = max over fluid particles i of case c of |a_i - b_i| * scale */
 aqua_status aqua_gnn_case_max_diff(uint32_t n_cases, const uint32_t* offsets,
                                    const float* a, const float* b,

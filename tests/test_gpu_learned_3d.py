@@ -82,6 +82,48 @@ def test_probes_pressure_matches_numpy(torch):
                                       None) == -1
 
 
+def lowbias32(x):
+    x = np.asarray(x, np.uint64) & 0xffffffff
+    x ^= x >> 16
+    x = (x * 0x7feb352d) & 0xffffffff
+    x ^= x >> 15
+    x = (x * 0x846ca68b) & 0xffffffff
+    x ^= x >> 16
+    return x
+
+
+@pytest.mark.parametrize("frac", [0.0, 0.1, 0.5, 1.0])
+def test_sample_max_diff_matches_numpy(torch, frac):
+    """The subsampled density check picks the particles whose hash of
+    (index, seed) is below frac * 2^32 and returns their largest scaled
+    difference; a NaN counts as infinite."""
+    from aquagpusph_gb300 import learned as Lm
+    L = Lm.lib()
+    rng = np.random.default_rng(int(frac * 10))
+    n = 100003
+    a = rng.normal(0, 1, n).astype(np.float32)
+    b = rng.normal(0, 1, n).astype(np.float32)
+    imove = rng.choice(np.array([1, 1, 1, -3, 0], np.int32), n)
+    seed = 0x9e3779b9
+    below = min(int(frac * 2.0 ** 32), 0xffffffff)
+    idx = np.arange(n, dtype=np.uint64)
+    take = (imove == 1) & (lowbias32(idx ^ lowbias32(seed)) < below)
+    ref = float((np.abs(a - b) * np.float32(0.25))[take].max()) if take.any() else 0.0
+    dev = lambda x: torch.from_numpy(x).cuda()
+    out = torch.empty(1, dtype=torch.float32, device="cuda")
+    assert L.aqua_gnn_sample_max_diff(n, Lm._p(dev(a)), Lm._p(dev(b)),
+                                      Lm._p(dev(imove)), seed, frac, 0.25,
+                                      Lm._p(out), None) == 0
+    assert float(out.item()) == ref
+    if take.any():
+        a2 = a.copy()
+        a2[np.nonzero(take)[0][0]] = np.nan
+        assert L.aqua_gnn_sample_max_diff(n, Lm._p(dev(a2)), Lm._p(dev(b)),
+                                          Lm._p(dev(imove)), seed, frac, 0.25,
+                                          Lm._p(out), None) == 0
+        assert float(out.item()) == np.inf
+
+
 def trained_model(torch, c, iters):
     from aquagpusph_gb300 import learned as Lm
     from aquagpusph_gb300.solver import Solver
