@@ -286,9 +286,13 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     // one operand buffer: the layer-1 input (128 x K1), then, once layer 1's
     // MMAs have completed, the 128 x 64 activations of layers 1 and 2 (and,
     // with SUM, the layer-3 output tile)
-    uint8_t* sA0 = sW3 + kW;
-    uint8_t* sA1 = sA0;
-    SumShared* ss = reinterpret_cast<SumShared*>(sA0 + edge_operand_bytes<K1>());
+    // two such buffers: the next tile's input is gathered into the other
+    // one while this tile's layers run
+    uint8_t* const sA0 = sW3 + kW;
+    constexpr uint32_t kOp = edge_operand_bytes<K1>();
+    uint8_t* sA1 = sA0;  // the current tile's buffer
+    SumShared* ss =
+        reinterpret_cast<SumShared*>(sA0 + 2u * edge_operand_bytes<K1>());
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     stage(sW1, W1, K1, 64, 64, K1);
@@ -417,33 +421,57 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     }
     const uint32_t tiles = SUM ? (e_end - e_begin + kTcRows - 1) / kTcRows
                                : (E + kTcRows - 1) / kTcRows;
-    for (uint32_t tile = SUM ? 0u : blockIdx.x; tile < tiles && !failed;
-         tile += SUM ? 1u : gridDim.x) {
-        const uint32_t eb = e_begin + tile * kTcRows;
-        const uint32_t e = eb + r;
+    // gathers the layer-1 input rows of tile t into buf (asynchronous
+    // copies, committed by the caller); returns this thread's receiver
+    // (~0 past the last edge)
+    constexpr uint32_t kg = K1 / 8;
+    auto gather = [&](uint32_t t, uint8_t* buf) -> uint32_t {
+        const uint32_t e = e_begin + t * kTcRows + r;
         const bool valid = e < e_end;
-        if constexpr (SUM)
-            ss->recv[r] = valid ? recv[e] : 0xffffffffu;
-        // layer-1 input rows, gathered asynchronously into sA0
-        constexpr uint32_t kg = K1 / 8;
-        uint8_t* row0 = sA0 + (r / 8) * kg * 128 + (r % 8) * 16;
+        uint8_t* row0 = buf + (r / 8) * kg * 128 + (r % 8) * 16;
+        uint32_t er = 0xffffffffu;
         if (PAIR) {
-            const uint32_t er = valid ? recv[e] : 0u, es = valid ? send[e] : 0u;
+            const uint32_t ei = valid ? recv[e] : 0u, es = valid ? send[e] : 0u;
             for (uint32_t g = 0; g < kg; g++) {
                 const uint16_t* src =
-                    g < 8 ? H + (size_t)er * ldh + g * 8
+                    g < 8 ? H + (size_t)ei * ldh + g * 8
                           : (g < 16 ? H + (size_t)es * ldh + (g - 8) * 8
                                     : Ef + (size_t)(valid ? e : 0u) * 16 + (g - 16) * 8);
                 cp_async_16z(row0 + g * 128, src, valid);
             }
+            if (valid)
+                er = ei;
         } else {
             for (uint32_t g = 0; g < kg; g++)
                 cp_async_16z(row0 + g * 128, X + (size_t)(valid ? e : 0u) * ldx + g * 8,
                              valid);
+            if (SUM && valid)
+                er = recv[e];
         }
+        return er;
+    };
+    const uint32_t stride = SUM ? 1u : gridDim.x;
+    uint32_t tile = SUM ? 0u : blockIdx.x;
+    uint32_t er_cur = 0xffffffffu;
+    uint32_t cur = 0;
+    if (tile < tiles)
+        er_cur = gather(tile, sA0);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    for (; tile < tiles && !failed; tile += stride) {
+        // the next tile's gather overlaps this tile's layers
+        const uint32_t next = tile + stride;
+        uint32_t er_next = 0xffffffffu;
+        if (next < tiles)
+            er_next = gather(next, sA0 + (cur ^ 1u) * kOp);
         asm volatile("cp.async.commit_group;\n" ::: "memory");
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        if (!layer(sA0, sW1, K1)) {
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        const uint32_t eb = e_begin + tile * kTcRows;
+        const uint32_t e = eb + r;
+        const bool valid = e < e_end;
+        sA1 = sA0 + cur * kOp;
+        if constexpr (SUM)
+            ss->recv[r] = er_cur;
+        if (!layer(sA1, sW1, K1)) {
             failed = true;
             break;
         }
@@ -523,10 +551,15 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
                 }
             }
         }
-        // the next tile's copies and MMAs reuse sA0, sA1 and the accumulator
+        // the tile after next reuses this buffer; the next tile's MMAs
+        // reuse the accumulator
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();
+        er_cur = er_next;
+        cur ^= 1u;
     }
+    // no copy may still be in flight when the CTA ends (after a time-out)
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n");
@@ -540,8 +573,12 @@ constexpr size_t
 edge_mlp_smem()
 {
     return ((64u * K1 * 2u + 1023u) / 1024u) * 1024u + 2u * 64u * 64u * 2u +
-           edge_operand_bytes<K1>() + (SUM ? sizeof(SumShared) : 0u);
+           2u * edge_operand_bytes<K1>() + (SUM ? sizeof(SumShared) : 0u);
 }
+static_assert(2 * (edge_mlp_smem<144, true>() + 1024) <= 228 * 1024,
+              "two pair-input CTAs per SM");
+static_assert(4 * (edge_mlp_smem<16, true>() + 1024) <= 228 * 1024,
+              "four row-input CTAs per SM");
 
 }  // namespace
 
@@ -623,15 +660,15 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
     const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
     cudaStream_t s = (cudaStream_t)stream;
     if (pair) {
-        // 72 KB of shared memory: three CTAs per SM (192 of 512 TMEM columns)
-        const uint32_t grid = tiles < (uint32_t)sms * 3u ? tiles : (uint32_t)sms * 3u;
+        // 106 KB of shared memory: two CTAs per SM (128 of 512 TMEM columns)
+        const uint32_t grid = tiles < (uint32_t)sms * 2u ? tiles : (uint32_t)sms * 2u;
         k_edge_mlp_tc<144, true, false>
             <<<grid, kTcThreads, edge_mlp_smem<144, false>(), s>>>(
                 E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
                 act1, act2, act3, Y, ldy, err, 0u, nullptr, 0.f, 0u);
     } else {
-        // 34 KB: at most six CTAs per SM (384 TMEM columns)
-        const uint32_t grid = tiles < (uint32_t)sms * 6u ? tiles : (uint32_t)sms * 6u;
+        // 50 KB: four CTAs per SM (256 TMEM columns)
+        const uint32_t grid = tiles < (uint32_t)sms * 4u ? tiles : (uint32_t)sms * 4u;
         k_edge_mlp_tc<16, false, false>
             <<<grid, kTcThreads, edge_mlp_smem<16, false>(), s>>>(
                 E, X, ldx, nullptr, nullptr, nullptr, 0, nullptr, W1, b1, W2,
@@ -667,7 +704,7 @@ aqua_gnn_edge_mlp_sum_tc(uint32_t n_nodes, uint32_t E, uint32_t K1,
     // each CTA owns the receivers of about E / grid edges; a small graph
     // gets fewer CTAs (at least one, for the receivers without edges)
     const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
-    const uint32_t per_sm = pair ? 3u : 6u;
+    const uint32_t per_sm = pair ? 2u : 4u;
     uint32_t grid = (uint32_t)sms * per_sm;
     if (tiles < grid)
         grid = tiles > 0 ? tiles : 1u;
