@@ -252,18 +252,33 @@ edge_operand_bytes()
     return a0 > a1 ? a0 : a1;
 }
 
-// the receiver-sum bookkeeping of a SUM CTA (shared memory after the
-// operand buffer)
-struct SumShared {
+// 8 warps: warps w and w + 4 read the same 32 tensor-memory lanes (rows
+// 32 (w % 4) ..), each one half of the 64 columns
+constexpr int kEdgeThreads = 256;
+constexpr int kEdgeWarps = kEdgeThreads / 32;
+
+// shared memory after the two operand buffers: the biases, and the
+// receiver-sum bookkeeping of a SUM CTA
+struct EdgeShared {
+    float bias[3][64];
     uint32_t recv[kTcRows];   // receiver of each row of the tile (~0: none)
-    uint32_t start[4];        // rows that start a receiver's run, per warp
+    uint32_t start[4];        // rows that start a receiver's run, per 32 rows
     float carry[2][64];       // partial sums carried into the next tile
     uint32_t carry_node[2];   // their receiver (~0: none)
     uint32_t nodes[2];        // this CTA's receivers [nodes[0], nodes[1])
 };
 
+// CTAs per SM: two with the 144-wide pair input (shared memory), three with
+// the 16-wide rows (registers)
+template<bool PAIR>
+constexpr int
+edge_ctas_per_sm()
+{
+    return PAIR ? 2 : 3;
+}
+
 template<int K1, bool PAIR, bool SUM>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kEdgeThreads, edge_ctas_per_sm<PAIR>())
 k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
               const uint32_t* __restrict__ recv, const uint32_t* __restrict__ send,
               const uint16_t* __restrict__ H, uint32_t ldh,
@@ -277,28 +292,40 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
 {
     constexpr uint32_t kW1 = ((64u * K1 * 2u + 1023u) / 1024u) * 1024u;
     constexpr uint32_t kW = 64u * 64u * 2u;            // W2, W3
+    constexpr uint32_t kOp = edge_operand_bytes<K1>();
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     uint8_t* sW1 = smem;
     uint8_t* sW2 = sW1 + kW1;
     uint8_t* sW3 = sW2 + kW;
-    // one operand buffer: the layer-1 input (128 x K1), then, once layer 1's
-    // MMAs have completed, the 128 x 64 activations of layers 1 and 2 (and,
-    // with SUM, the layer-3 output tile)
-    // two such buffers: the next tile's input is gathered into the other
-    // one while this tile's layers run
+    // an operand buffer holds the layer-1 input (128 x K1), then, once
+    // layer 1's MMAs have completed, the 128 x 64 activations of layers 1
+    // and 2 (and, with SUM, the layer-3 output tile); of the two buffers,
+    // the next tile's input is gathered into the other one while this
+    // tile's layers run
     uint8_t* const sA0 = sW3 + kW;
-    constexpr uint32_t kOp = edge_operand_bytes<K1>();
     uint8_t* sA1 = sA0;  // the current tile's buffer
-    SumShared* ss =
-        reinterpret_cast<SumShared*>(sA0 + 2u * edge_operand_bytes<K1>());
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    EdgeShared* ss = reinterpret_cast<EdgeShared*>(sA0 + 2u * kOp);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t warp = tid >> 5, lane = tid & 31;
 
-    stage(sW1, W1, K1, 64, 64, K1);
-    stage(sW2, W2, 64, 64, 64, 64);
-    stage(sW3, W3, 64, 64, 64, 64);
-    if (threadIdx.x == 0)
+    for (uint32_t e = tid; e < 64u * K1 / 8u; e += kEdgeThreads) {
+        const uint32_t row = e / (K1 / 8), g = e % (K1 / 8);
+        *reinterpret_cast<uint4*>(sW1 + ((row / 8) * (K1 / 8) + g) * 128 + (row % 8) * 16) =
+            *reinterpret_cast<const uint4*>(W1 + (size_t)row * K1 + g * 8);
+    }
+    for (uint32_t e = tid; e < 64u * 8u; e += kEdgeThreads) {
+        const uint32_t row = e / 8, g = e % 8;
+        const uint32_t o = ((row / 8) * 8 + g) * 128 + (row % 8) * 16;
+        *reinterpret_cast<uint4*>(sW2 + o) =
+            *reinterpret_cast<const uint4*>(W2 + (size_t)row * 64 + g * 8);
+        *reinterpret_cast<uint4*>(sW3 + o) =
+            *reinterpret_cast<const uint4*>(W3 + (size_t)row * 64 + g * 8);
+    }
+    if (tid < 192)
+        ss->bias[tid / 64][tid % 64] = (tid < 64 ? b1 : (tid < 128 ? b2 : b3))[tid % 64];
+    if (tid == 0)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_addr(&mbar)));
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 "
@@ -318,7 +345,7 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n");
             const uint32_t sbo = (K / 8) * 128;
             for (uint32_t ks = 0; ks < K / 16; ks++) {
@@ -348,46 +375,54 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         asm volatile("tcgen05.fence::after_thread_sync;\n");
         return !bad;
     };
-    // read the accumulator row of this thread, add the bias, activate;
+    // this thread's row of the accumulator and half of its columns
+    const uint32_t row = (warp & 3u) * 32u + lane;
+    const uint32_t half = warp >> 2;
+    // read the accumulator (32 columns), add the bias, activate;
     // `emit(g, packed8)` receives the row's k-group g (8 bf16 as a uint4)
-    auto epilogue = [&](const float* __restrict__ bias, int act, auto&& emit) {
-        const uint32_t taddr = tmem + ((warp * 32u) << 16);
+    auto epilogue = [&](int layer_index, int act, auto&& emit) {
+        const uint32_t taddr = tmem + (((warp & 3u) * 32u) << 16) + half * 32u;
+        uint32_t v[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+              "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+              "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+              "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+              "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+              "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+              "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+        const float* bias = ss->bias[layer_index] + half * 32u;
 #pragma unroll
-        for (int c0 = 0; c0 < 64; c0 += 16) {
-            uint32_t v[16];
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
-                  "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
-                  "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                  "=r"(v[14]), "=r"(v[15])
-                : "r"(taddr + (uint32_t)c0));
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
-            uint32_t p[8];
-            for (int j = 0; j < 8; j++) {
-                float z0 = __uint_as_float(v[2 * j]) + bias[c0 + 2 * j];
-                float z1 = __uint_as_float(v[2 * j + 1]) + bias[c0 + 2 * j + 1];
+        for (int q = 0; q < 4; q++) {
+            uint32_t p[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int c = q * 8 + 2 * j;
+                float z0 = __uint_as_float(v[c]) + bias[c];
+                float z1 = __uint_as_float(v[c + 1]) + bias[c + 1];
                 if (act == AQUA_ACT_SILU) {
                     z0 = silu_f(z0);
                     z1 = silu_f(z1);
                 }
                 p[j] = pack2(z0, z1);
             }
-            emit(c0 / 8, make_uint4(p[0], p[1], p[2], p[3]));
-            emit(c0 / 8 + 1, make_uint4(p[4], p[5], p[6], p[7]));
+            emit((int)(half * 4u) + q, make_uint4(p[0], p[1], p[2], p[3]));
         }
     };
-    const uint32_t r = threadIdx.x;  // this thread's row of the tile
     auto to_a1 = [&](int g, uint4 val) {
-        *reinterpret_cast<uint4*>(sA1 + ((r / 8) * 8 + g) * 128 + (r % 8) * 16) = val;
+        *reinterpret_cast<uint4*>(sA1 + ((row / 8) * 8 + g) * 128 + (row % 8) * 16) = val;
     };
 
     // the edges of this CTA: every tile (grid-stride), or, with SUM, the
     // edges of its receivers
     uint32_t e_begin = 0, e_end = E;
     if constexpr (SUM) {
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             // first node s in [0, n_nodes] with off[s] >= v
             auto lower = [&](uint64_t v) -> uint32_t {
                 uint32_t lo = 0, hi = n_nodes;
@@ -410,7 +445,7 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         __syncthreads();
         const uint32_t n_lo = ss->nodes[0], n_hi = ss->nodes[1];
         // receivers without edges: a zero sum
-        for (uint32_t s = n_lo + threadIdx.x; s < n_hi; s += kTcThreads)
+        for (uint32_t s = n_lo + tid; s < n_hi; s += kEdgeThreads)
             if (off[s] == off[s + 1]) {
                 uint4* dst = reinterpret_cast<uint4*>(Y + (size_t)s * ldy + col);
                 for (int g = 0; g < 8; g++)
@@ -421,18 +456,22 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     }
     const uint32_t tiles = SUM ? (e_end - e_begin + kTcRows - 1) / kTcRows
                                : (E + kTcRows - 1) / kTcRows;
-    // gathers the layer-1 input rows of tile t into buf (asynchronous
-    // copies, committed by the caller); returns this thread's receiver
-    // (~0 past the last edge)
+    // gathers the layer-1 input of tile t into buf: thread t copies k-groups
+    // [part * kg / 2, (part + 1) * kg / 2) of row t % 128 (asynchronous
+    // copies, committed by the caller); returns the row's receiver for the
+    // threads of the first part (~0 past the last edge)
     constexpr uint32_t kg = K1 / 8;
+    const uint32_t grow = tid % kTcRows, part = tid / kTcRows;
     auto gather = [&](uint32_t t, uint8_t* buf) -> uint32_t {
-        const uint32_t e = e_begin + t * kTcRows + r;
+        const uint32_t e = e_begin + t * kTcRows + grow;
         const bool valid = e < e_end;
-        uint8_t* row0 = buf + (r / 8) * kg * 128 + (r % 8) * 16;
+        uint8_t* row0 = buf + (grow / 8) * kg * 128 + (grow % 8) * 16;
+        const uint32_t g0 = part * (kg / 2), g1 = g0 + kg / 2;
         uint32_t er = 0xffffffffu;
         if (PAIR) {
-            const uint32_t ei = valid ? recv[e] : 0u, es = valid ? send[e] : 0u;
-            for (uint32_t g = 0; g < kg; g++) {
+            const uint32_t ei = (valid && part == 0) ? recv[e] : 0u;
+            const uint32_t es = valid ? send[e] : 0u;
+            for (uint32_t g = g0; g < g1; g++) {
                 const uint16_t* src =
                     g < 8 ? H + (size_t)ei * ldh + g * 8
                           : (g < 16 ? H + (size_t)es * ldh + (g - 8) * 8
@@ -442,10 +481,10 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
             if (valid)
                 er = ei;
         } else {
-            for (uint32_t g = 0; g < kg; g++)
+            for (uint32_t g = g0; g < g1; g++)
                 cp_async_16z(row0 + g * 128, X + (size_t)(valid ? e : 0u) * ldx + g * 8,
                              valid);
-            if (SUM && valid)
+            if (SUM && valid && part == 0)
                 er = recv[e];
         }
         return er;
@@ -466,41 +505,44 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         asm volatile("cp.async.commit_group;\n" ::: "memory");
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         const uint32_t eb = e_begin + tile * kTcRows;
-        const uint32_t e = eb + r;
+        const uint32_t e = eb + row;
         const bool valid = e < e_end;
         sA1 = sA0 + cur * kOp;
-        if constexpr (SUM)
-            ss->recv[r] = er_cur;
+        if (SUM && part == 0)
+            ss->recv[grow] = er_cur;
         if (!layer(sA1, sW1, K1)) {
             failed = true;
             break;
         }
-        epilogue(b1, act1, to_a1);
+        epilogue(0, act1, to_a1);
         if (!layer(sA1, sW2, 64)) {
             failed = true;
             break;
         }
-        epilogue(b2, act2, to_a1);
+        epilogue(1, act2, to_a1);
         if (!layer(sA1, sW3, 64)) {
             failed = true;
             break;
         }
         if constexpr (!SUM) {
-            epilogue(b3, act3, [&](int g, uint4 val) {
+            epilogue(2, act3, [&](int g, uint4 val) {
                 if (valid)
                     *reinterpret_cast<uint4*>(Y + (size_t)e * ldy + g * 8) = val;
             });
         } else {
             // layer-3 tile into shared memory: row r at r * 128 bytes, its
             // 16-byte group g at position g ^ (r % 8)
-            epilogue(b3, act3, [&](int g, uint4 val) {
-                *reinterpret_cast<uint4*>(sA1 + r * 128u + ((g ^ (r & 7u)) * 16u)) = val;
+            epilogue(2, act3, [&](int g, uint4 val) {
+                *reinterpret_cast<uint4*>(sA1 + row * 128u + ((g ^ (row & 7u)) * 16u)) = val;
             });
             const uint32_t nvalid = min((uint32_t)kTcRows, e_end - eb);
-            const bool st = r < nvalid && (r == 0 || ss->recv[r] != ss->recv[r - 1]);
-            const uint32_t bal = __ballot_sync(0xffffffffu, st);
-            if (lane == 0)
-                ss->start[warp] = bal;
+            if (warp < 4) {
+                const uint32_t rr = warp * 32u + lane;
+                const bool st = rr < nvalid && (rr == 0 || ss->recv[rr] != ss->recv[rr - 1]);
+                const uint32_t bal = __ballot_sync(0xffffffffu, st);
+                if (lane == 0)
+                    ss->start[warp] = bal;
+            }
             __syncthreads();
             const uint32_t par = tile & 1u;
             uint32_t ord = 0;
@@ -509,7 +551,7 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
                 while (m) {
                     const uint32_t a = wq * 32u + (uint32_t)(__ffs(m) - 1);
                     m &= m - 1;
-                    if ((ord++ & 3u) != warp)
+                    if ((ord++ % kEdgeWarps) != warp)
                         continue;
                     // the run ends at the next start or at the last row
                     uint32_t b = nvalid;
@@ -568,17 +610,17 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     }
 }
 
-template<int K1, bool SUM>
+template<int K1>
 constexpr size_t
 edge_mlp_smem()
 {
     return ((64u * K1 * 2u + 1023u) / 1024u) * 1024u + 2u * 64u * 64u * 2u +
-           2u * edge_operand_bytes<K1>() + (SUM ? sizeof(SumShared) : 0u);
+           2u * edge_operand_bytes<K1>() + sizeof(EdgeShared);
 }
-static_assert(2 * (edge_mlp_smem<144, true>() + 1024) <= 228 * 1024,
-              "two pair-input CTAs per SM");
-static_assert(4 * (edge_mlp_smem<16, true>() + 1024) <= 228 * 1024,
-              "four row-input CTAs per SM");
+static_assert(edge_ctas_per_sm<true>() * (edge_mlp_smem<144>() + 1024) <= 228 * 1024,
+              "pair-input CTAs per SM");
+static_assert(edge_ctas_per_sm<false>() * (edge_mlp_smem<16>() + 1024) <= 228 * 1024,
+              "row-input CTAs per SM");
 
 }  // namespace
 
@@ -599,13 +641,13 @@ edge_mlp_configure(int& sms)
     if (!bit || !(configured.load() & bit)) {
         const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
         if (cudaFuncSetAttribute(k_edge_mlp_tc<16, false, false>, a,
-                                 (int)edge_mlp_smem<16, false>()) != cudaSuccess ||
+                                 (int)edge_mlp_smem<16>()) != cudaSuccess ||
             cudaFuncSetAttribute(k_edge_mlp_tc<144, true, false>, a,
-                                 (int)edge_mlp_smem<144, false>()) != cudaSuccess ||
+                                 (int)edge_mlp_smem<144>()) != cudaSuccess ||
             cudaFuncSetAttribute(k_edge_mlp_tc<16, false, true>, a,
-                                 (int)edge_mlp_smem<16, true>()) != cudaSuccess ||
+                                 (int)edge_mlp_smem<16>()) != cudaSuccess ||
             cudaFuncSetAttribute(k_edge_mlp_tc<144, true, true>, a,
-                                 (int)edge_mlp_smem<144, true>()) != cudaSuccess)
+                                 (int)edge_mlp_smem<144>()) != cudaSuccess)
             return AQUA_ERR_CUDA;
         configured.fetch_or(bit);
     }
@@ -660,17 +702,19 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
     const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
     cudaStream_t s = (cudaStream_t)stream;
     if (pair) {
-        // 106 KB of shared memory: two CTAs per SM (128 of 512 TMEM columns)
-        const uint32_t grid = tiles < (uint32_t)sms * 2u ? tiles : (uint32_t)sms * 2u;
+        // 108 KB of shared memory: two CTAs per SM (128 of 512 TMEM columns)
+        const uint32_t cap = (uint32_t)sms * edge_ctas_per_sm<true>();
+        const uint32_t grid = tiles < cap ? tiles : cap;
         k_edge_mlp_tc<144, true, false>
-            <<<grid, kTcThreads, edge_mlp_smem<144, false>(), s>>>(
+            <<<grid, kEdgeThreads, edge_mlp_smem<144>(), s>>>(
                 E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
                 act1, act2, act3, Y, ldy, err, 0u, nullptr, 0.f, 0u);
     } else {
-        // 50 KB: four CTAs per SM (256 TMEM columns)
-        const uint32_t grid = tiles < (uint32_t)sms * 4u ? tiles : (uint32_t)sms * 4u;
+        // 52 KB: three CTAs per SM (registers; 192 TMEM columns)
+        const uint32_t cap = (uint32_t)sms * edge_ctas_per_sm<false>();
+        const uint32_t grid = tiles < cap ? tiles : cap;
         k_edge_mlp_tc<16, false, false>
-            <<<grid, kTcThreads, edge_mlp_smem<16, false>(), s>>>(
+            <<<grid, kEdgeThreads, edge_mlp_smem<16>(), s>>>(
                 E, X, ldx, nullptr, nullptr, nullptr, 0, nullptr, W1, b1, W2,
                 b2, W3, b3, act1, act2, act3, Y, ldy, err, 0u, nullptr, 0.f, 0u);
     }
@@ -704,19 +748,20 @@ aqua_gnn_edge_mlp_sum_tc(uint32_t n_nodes, uint32_t E, uint32_t K1,
     // each CTA owns the receivers of about E / grid edges; a small graph
     // gets fewer CTAs (at least one, for the receivers without edges)
     const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
-    const uint32_t per_sm = pair ? 2u : 4u;
+    const uint32_t per_sm = (uint32_t)(pair ? edge_ctas_per_sm<true>()
+                                             : edge_ctas_per_sm<false>());
     uint32_t grid = (uint32_t)sms * per_sm;
     if (tiles < grid)
         grid = tiles > 0 ? tiles : 1u;
     cudaStream_t s = (cudaStream_t)stream;
     if (pair)
         k_edge_mlp_tc<144, true, true>
-            <<<grid, kTcThreads, edge_mlp_smem<144, true>(), s>>>(
+            <<<grid, kEdgeThreads, edge_mlp_smem<144>(), s>>>(
                 E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
                 act1, act2, act3, out, ld, err, n_nodes, offsets, scale, col);
     else
         k_edge_mlp_tc<16, false, true>
-            <<<grid, kTcThreads, edge_mlp_smem<16, true>(), s>>>(
+            <<<grid, kEdgeThreads, edge_mlp_smem<16>(), s>>>(
                 E, X, ldx, recv, nullptr, nullptr, 0, nullptr, W1, b1, W2, b2,
                 W3, b3, act1, act2, act3, out, ld, err, n_nodes, offsets, scale,
                 col);
