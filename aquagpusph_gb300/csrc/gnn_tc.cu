@@ -268,13 +268,20 @@ struct EdgeShared {
     uint32_t nodes[2];        // this CTA's receivers [nodes[0], nodes[1])
 };
 
-// CTAs per SM: two with the 144-wide pair input (shared memory), three with
-// the 16-wide rows (registers)
+// CTAs per SM: three of 256 threads (registers); operand buffers per CTA:
+// one with the 144-wide pair input (shared memory), two with the 16-wide
+// rows (the next tile's rows are gathered during this tile's layers)
 template<bool PAIR>
-constexpr int
+__host__ __device__ constexpr int
 edge_ctas_per_sm()
 {
-    return PAIR ? 2 : 3;
+    return 3;
+}
+template<bool PAIR>
+__host__ __device__ constexpr uint32_t
+edge_buffers()
+{
+    return PAIR ? 1u : 2u;
 }
 
 template<int K1, bool PAIR, bool SUM>
@@ -304,9 +311,10 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     // and 2 (and, with SUM, the layer-3 output tile); of the two buffers,
     // the next tile's input is gathered into the other one while this
     // tile's layers run
+    constexpr uint32_t kBufs = edge_buffers<PAIR>();
     uint8_t* const sA0 = sW3 + kW;
     uint8_t* sA1 = sA0;  // the current tile's buffer
-    EdgeShared* ss = reinterpret_cast<EdgeShared*>(sA0 + 2u * kOp);
+    EdgeShared* ss = reinterpret_cast<EdgeShared*>(sA0 + kBufs * kOp);
     const uint32_t tid = threadIdx.x;
     const uint32_t warp = tid >> 5, lane = tid & 31;
 
@@ -493,17 +501,23 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     uint32_t tile = SUM ? 0u : blockIdx.x;
     uint32_t er_cur = 0xffffffffu;
     uint32_t cur = 0;
-    if (tile < tiles)
+    if (kBufs == 2 && tile < tiles)
         er_cur = gather(tile, sA0);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     for (; tile < tiles && !failed; tile += stride) {
-        // the next tile's gather overlaps this tile's layers
         const uint32_t next = tile + stride;
         uint32_t er_next = 0xffffffffu;
-        if (next < tiles)
-            er_next = gather(next, sA0 + (cur ^ 1u) * kOp);
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        if constexpr (kBufs == 2) {
+            // the next tile's gather overlaps this tile's layers
+            if (next < tiles)
+                er_next = gather(next, sA0 + (cur ^ 1u) * kOp);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            er_cur = gather(tile, sA0);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
         const uint32_t eb = e_begin + tile * kTcRows;
         const uint32_t e = eb + row;
         const bool valid = e < e_end;
@@ -598,7 +612,7 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();
         er_cur = er_next;
-        cur ^= 1u;
+        cur = (cur + 1u) % kBufs;
     }
     // no copy may still be in flight when the CTA ends (after a time-out)
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -615,7 +629,7 @@ constexpr size_t
 edge_mlp_smem()
 {
     return ((64u * K1 * 2u + 1023u) / 1024u) * 1024u + 2u * 64u * 64u * 2u +
-           2u * edge_operand_bytes<K1>() + sizeof(EdgeShared);
+           edge_buffers<K1 == 144>() * edge_operand_bytes<K1>() + sizeof(EdgeShared);
 }
 static_assert(edge_ctas_per_sm<true>() * (edge_mlp_smem<144>() + 1024) <= 228 * 1024,
               "pair-input CTAs per SM");
@@ -702,7 +716,7 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
     const uint32_t tiles = (E + kTcRows - 1) / kTcRows;
     cudaStream_t s = (cudaStream_t)stream;
     if (pair) {
-        // 108 KB of shared memory: two CTAs per SM (128 of 512 TMEM columns)
+        // 72 KB of shared memory: three CTAs per SM (192 of 512 TMEM columns)
         const uint32_t cap = (uint32_t)sms * edge_ctas_per_sm<true>();
         const uint32_t grid = tiles < cap ? tiles : cap;
         k_edge_mlp_tc<144, true, false>
