@@ -266,6 +266,7 @@ struct EdgeShared {
     float carry[2][64];       // partial sums carried into the next tile
     uint32_t carry_node[2];   // their receiver (~0: none)
     uint32_t nodes[2];        // this CTA's receivers [nodes[0], nodes[1])
+    uint32_t next_recv;       // receiver of the edge after the tile (~0: none)
 };
 
 // CTAs per SM: three of 256 threads (registers); operand buffers per CTA:
@@ -464,57 +465,68 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     }
     const uint32_t tiles = SUM ? (e_end - e_begin + kTcRows - 1) / kTcRows
                                : (E + kTcRows - 1) / kTcRows;
-    // gathers the layer-1 input of tile t into buf: thread t copies k-groups
-    // [part * kg / 2, (part + 1) * kg / 2) of row t % 128 (asynchronous
-    // copies, committed by the caller); returns the row's receiver for the
-    // threads of the first part (~0 past the last edge)
+    // the edge indices of tile t's rows, loaded one tile ahead: the
+    // receiver (threads of the first part; ~0 past the last edge) and the
+    // sender (pair input)
     constexpr uint32_t kg = K1 / 8;
     const uint32_t grow = tid % kTcRows, part = tid / kTcRows;
-    auto gather = [&](uint32_t t, uint8_t* buf) -> uint32_t {
+    auto load_idx = [&](uint32_t t, uint32_t& ei, uint32_t& es) {
+        ei = 0xffffffffu;
+        es = 0u;
+        if (t >= tiles)
+            return;
+        const uint32_t e = e_begin + t * kTcRows + grow;
+        if (e >= e_end)
+            return;
+        if ((PAIR || SUM) && part == 0)
+            ei = recv[e];
+        if (PAIR)
+            es = send[e];
+    };
+    // gathers the layer-1 input of tile t into buf: thread t copies k-groups
+    // [part * kg / 2, (part + 1) * kg / 2) of row t % 128 (asynchronous
+    // copies, committed by the caller)
+    auto gather = [&](uint32_t t, uint8_t* buf, uint32_t ei, uint32_t es) {
         const uint32_t e = e_begin + t * kTcRows + grow;
         const bool valid = e < e_end;
         uint8_t* row0 = buf + (grow / 8) * kg * 128 + (grow % 8) * 16;
         const uint32_t g0 = part * (kg / 2), g1 = g0 + kg / 2;
-        uint32_t er = 0xffffffffu;
         if (PAIR) {
-            const uint32_t ei = (valid && part == 0) ? recv[e] : 0u;
-            const uint32_t es = valid ? send[e] : 0u;
+            const uint32_t eiv = (valid && part == 0) ? ei : 0u;
+            const uint32_t esv = valid ? es : 0u;
             for (uint32_t g = g0; g < g1; g++) {
                 const uint16_t* src =
-                    g < 8 ? H + (size_t)ei * ldh + g * 8
-                          : (g < 16 ? H + (size_t)es * ldh + (g - 8) * 8
+                    g < 8 ? H + (size_t)eiv * ldh + g * 8
+                          : (g < 16 ? H + (size_t)esv * ldh + (g - 8) * 8
                                     : Ef + (size_t)(valid ? e : 0u) * 16 + (g - 16) * 8);
                 cp_async_16z(row0 + g * 128, src, valid);
             }
-            if (valid)
-                er = ei;
         } else {
             for (uint32_t g = g0; g < g1; g++)
                 cp_async_16z(row0 + g * 128, X + (size_t)(valid ? e : 0u) * ldx + g * 8,
                              valid);
-            if (SUM && valid && part == 0)
-                er = recv[e];
         }
-        return er;
     };
     const uint32_t stride = SUM ? 1u : gridDim.x;
     uint32_t tile = SUM ? 0u : blockIdx.x;
-    uint32_t er_cur = 0xffffffffu;
+    uint32_t ei_cur, es_cur;
+    load_idx(tile, ei_cur, es_cur);
     uint32_t cur = 0;
     if (kBufs == 2 && tile < tiles)
-        er_cur = gather(tile, sA0);
+        gather(tile, sA0, ei_cur, es_cur);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     for (; tile < tiles && !failed; tile += stride) {
         const uint32_t next = tile + stride;
-        uint32_t er_next = 0xffffffffu;
+        uint32_t ei_next, es_next;
+        load_idx(next, ei_next, es_next);
         if constexpr (kBufs == 2) {
             // the next tile's gather overlaps this tile's layers
             if (next < tiles)
-                er_next = gather(next, sA0 + (cur ^ 1u) * kOp);
+                gather(next, sA0 + (cur ^ 1u) * kOp, ei_next, es_next);
             asm volatile("cp.async.commit_group;\n" ::: "memory");
             asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         } else {
-            er_cur = gather(tile, sA0);
+            gather(tile, sA0, ei_cur, es_cur);
             asm volatile("cp.async.commit_group;\n" ::: "memory");
             asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         }
@@ -523,7 +535,11 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         const bool valid = e < e_end;
         sA1 = sA0 + cur * kOp;
         if (SUM && part == 0)
-            ss->recv[grow] = er_cur;
+            ss->recv[grow] = ei_cur;
+        // the receiver of the edge after this tile's (~0 at the end of the
+        // CTA's edges): it tells whether the tile's last run is complete
+        if (SUM && tid == 0)
+            ss->next_recv = ei_next;
         if (!layer(sA1, sW1, K1)) {
             failed = true;
             break;
@@ -593,7 +609,7 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
                         a0 += __uint_as_float(v << 16);
                         a1 += __uint_as_float(v & 0xffff0000u);
                     }
-                    if (off[node + 1] <= eb + nvalid) {
+                    if (b < nvalid || ss->next_recv != node) {
                         *reinterpret_cast<uint32_t*>(Y + (size_t)node * ldy + col +
                                                      2 * lane) =
                             pack2(a0 * scale, a1 * scale);
@@ -611,7 +627,8 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         // reuse the accumulator
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();
-        er_cur = er_next;
+        ei_cur = ei_next;
+        es_cur = es_next;
         cur = (cur + 1u) % kBufs;
     }
     // no copy may still be in flight when the CTA ends (after a time-out)
