@@ -858,6 +858,56 @@ def run_learned_3d(args):
     return 0
 
 
+def run_forward_only(args):
+    """The network forward alone on the 64-tank batch (c3) or the 26M-particle
+    dam break (c5), untrained weights, after a few plain steps: one warm-up
+    forward, then one timed with CUDA events (for kernel launch lists)."""
+    import torch
+    from aquagpusph_gb300 import case as cases
+    from aquagpusph_gb300 import learned as Lm
+    from aquagpusph_gb300.solver import Solver
+    torch.cuda.set_device(0)
+    if args.workload == "c5":
+        c, _ = workload("c4")
+        dims, radius, cid = 3, 0.9 * c.params.h, None
+        sv = Solver(c.params, capacity=c.N)
+        sv.set_case(c)
+    else:
+        eb = cases.sloshing_batch_2d()
+        c = eb.case
+        dims, radius = 2, float(c.params.support * c.params.h)
+        sv = Solver(c.params, capacity=c.N,
+                    ihoc_capacity=eb.n_cases * c.params.max_cells())
+        sv.set_batch(eb)
+        cid = Lm.case_ids(eb)
+    if cid is None:
+        cid = torch.zeros(c.N, dtype=torch.int32, device="cuda")
+    sv.step(20, graph=True)
+    sv.check()
+    model = Lm.Model(dims, seed=0)
+    s0 = Lm.Snapshot.capture(sv, dims)
+    g = Lm.Graph(sv, dims, s0["r"], s0["imove"], cid, s0.n, radius)
+    x = Lm.Inputs(g, s0["r"], s0["u"], s0["rho"], s0["dudt"], s0["drhodt"],
+                  s0["imove"], s0["normal"])
+    net = Lm.Network(model, g, x)
+    net.forward()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    net.forward()
+    e1.record()
+    e1.synchronize()
+    flops = sum(2 * (g.n_edges if name[0] == "e" else g.n_nodes) * n * kk
+                for name, n, kk, act in Lm.LAYERS)
+    ms = e0.elapsed_time(e1)
+    print(json.dumps({"workload": workload_desc(args.workload),
+                      "forward_ms": ms, "edges": g.n_edges, "nodes": g.n_nodes,
+                      "flops": flops, "tflops": flops / (ms * 1e-3) / 1e12}),
+          flush=True)
+    sv.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -877,6 +927,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="minimum CPU work of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forward-only", action="store_true",
+                    help="c3 / c5: time the network forward alone")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -884,6 +936,8 @@ def main():
         return run_reference(args)
     if args.eval_warm is None:
         args.eval_warm = 200 if args.workload == "c5" else 3000
+    if args.forward_only and args.workload in ("c3", "c5"):
+        return run_forward_only(args)
     if args.workload == "c3":
         return run_learned(args)
     if args.workload == "c5":
