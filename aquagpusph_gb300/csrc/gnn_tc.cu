@@ -602,10 +602,27 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
                         a0 = ss->carry[par][2 * lane];
                         a1 = ss->carry[par][2 * lane + 1];
                     }
-                    for (uint32_t k = a; k < b; k++) {
-                        const uint32_t v = *reinterpret_cast<const uint32_t*>(
+                    // row k's two columns of this lane
+                    auto ld_row = [&](uint32_t k) -> uint32_t {
+                        return *reinterpret_cast<const uint32_t*>(
                             sA1 + k * 128u + (((lane >> 2) ^ (k & 7u)) * 16u) +
                             (lane & 3u) * 4u);
+                    };
+                    // eight loads in flight, then the additions in row order
+                    uint32_t k = a;
+                    for (; k + 8u <= b; k += 8u) {
+                        uint32_t v[8];
+#pragma unroll
+                        for (int u = 0; u < 8; u++)
+                            v[u] = ld_row(k + u);
+#pragma unroll
+                        for (int u = 0; u < 8; u++) {
+                            a0 += __uint_as_float(v[u] << 16);
+                            a1 += __uint_as_float(v[u] & 0xffff0000u);
+                        }
+                    }
+                    for (; k < b; k++) {
+                        const uint32_t v = ld_row(k);
                         a0 += __uint_as_float(v << 16);
                         a1 += __uint_as_float(v & 0xffff0000u);
                     }
