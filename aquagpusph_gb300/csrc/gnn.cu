@@ -477,6 +477,98 @@ k_edge_features(uint32_t E, int dims, const uint32_t* __restrict__ recv,
     }
 }
 
+// The node data the edge features read, packed per node into 16-byte
+// aligned records (2-D: 2 float4 = r, u | rho, imove bits, normal; 3-D:
+// 3 float4 = r, rho | u, imove bits | normal, 0), so that an edge reads two
+// or three aligned 16-byte words per end instead of ten scattered fields.
+template<int D>
+__global__ void
+k_node_records(uint32_t n, const float* __restrict__ r,
+               const float* __restrict__ u, const float* __restrict__ rho,
+               const int32_t* __restrict__ imove,
+               const float* __restrict__ normal, float4* rec)
+{
+    constexpr int VS = D == 3 ? 4 : 2;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n;
+         s += gridDim.x * blockDim.x) {
+        const float* rs = r + (size_t)s * VS;
+        const float* us = u + (size_t)s * VS;
+        const float* ns = normal + (size_t)s * VS;
+        const float im = __int_as_float(imove[s]);
+        if (D == 2) {
+            rec[(size_t)s * 2] = make_float4(rs[0], rs[1], us[0], us[1]);
+            rec[(size_t)s * 2 + 1] = make_float4(rho[s], im, ns[0], ns[1]);
+        } else {
+            rec[(size_t)s * 3] = make_float4(rs[0], rs[1], rs[2], rho[s]);
+            rec[(size_t)s * 3 + 1] = make_float4(us[0], us[1], us[2], im);
+            rec[(size_t)s * 3 + 2] = make_float4(ns[0], ns[1], ns[2], 0.f);
+        }
+    }
+}
+
+// k_edge_features from the packed records: the same features, computed by
+// the same operations in the same order
+template<int D>
+__global__ void
+k_edge_features_rec(uint32_t E, const uint32_t* __restrict__ recv,
+                    const uint32_t* __restrict__ send,
+                    const float4* __restrict__ rec,
+                    const float* __restrict__ sc, uint16_t* out)
+{
+    constexpr int NR = D == 3 ? 3 : 2;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < E;
+         e += gridDim.x * blockDim.x) {
+        const uint32_t i = recv[e], j = send[e];
+        float4 a[NR], b[NR];
+        for (int q = 0; q < NR; q++) {
+            a[q] = rec[(size_t)i * NR + q];
+            b[q] = rec[(size_t)j * NR + q];
+        }
+        float ri[3], rj[3], ui[3], uj[3], nj[3];
+        float rhoi, rhoj;
+        int imj;
+        if (D == 2) {
+            ri[0] = a[0].x; ri[1] = a[0].y; ui[0] = a[0].z; ui[1] = a[0].w;
+            rj[0] = b[0].x; rj[1] = b[0].y; uj[0] = b[0].z; uj[1] = b[0].w;
+            rhoi = a[1].x;
+            rhoj = b[1].x;
+            imj = __float_as_int(b[1].y);
+            nj[0] = b[1].z; nj[1] = b[1].w;
+        } else {
+            ri[0] = a[0].x; ri[1] = a[0].y; ri[2] = a[0].z; rhoi = a[0].w;
+            rj[0] = b[0].x; rj[1] = b[0].y; rj[2] = b[0].z; rhoj = b[0].w;
+            ui[0] = a[1].x; ui[1] = a[1].y; ui[2] = a[1].z;
+            uj[0] = b[1].x; uj[1] = b[1].y; uj[2] = b[1].z;
+            imj = __float_as_int(b[1].w);
+            nj[0] = b[2].x; nj[1] = b[2].y; nj[2] = b[2].z;
+        }
+        float f[AQUA_GNN_FEATURES];
+        for (int k = 0; k < AQUA_GNN_FEATURES; k++)
+            f[k] = 0.f;
+        const float h = sc[0], U = sc[1], R = sc[2];
+        int k = 0;
+        float rr = 0.f;
+        for (int d = 0; d < D; d++) {
+            const float dd = rj[d] - ri[d];
+            rr += dd * dd;
+            f[k++] = dd / h;
+        }
+        const float q = sqrtf(rr) / h;
+        f[k++] = q;
+        for (int d = 0; d < D; d++)
+            f[k++] = (uj[d] - ui[d]) / U;
+        f[k++] = (rhoj - rhoi) / R;
+        f[k++] = wendland_shape(q);
+        const bool wall = imj < 0;
+        f[k++] = wall ? 1.f : 0.f;
+        for (int d = 0; d < D; d++)
+            f[k++] = wall ? nj[d] : 0.f;
+        uint16_t* row = out + (size_t)e * AQUA_GNN_FEATURES;
+        for (int m = 0; m < AQUA_GNN_FEATURES; m += 2)
+            *reinterpret_cast<uint32_t*>(row + m) = pack_bf2(f[m], f[m + 1]);
+    }
+}
+
 // ---------------------------------------------------------- dense layers ----
 
 constexpr int kLinThreads = 128;  // 4 warps, 16 rows each per tile
@@ -1330,6 +1422,47 @@ aqua_gnn_edge_features(uint32_t E, int32_t dims, const uint32_t* recv,
         return AQUA_OK;
     k_edge_features<<<blocks_for(E, 256), 256, 0, (cudaStream_t)stream>>>(
         E, dims, recv, send, r, u, rho, imove, normal, scales, out);
+    return last_error();
+}
+
+aqua_status
+aqua_gnn_node_records(uint32_t n, int32_t dims, const float* r, const float* u,
+                      const float* rho, const int32_t* imove,
+                      const float* normal, float* rec, void* stream)
+{
+    if ((dims != 2 && dims != 3) || !r || !u || !rho || !imove || !normal ||
+        !rec || (reinterpret_cast<uintptr_t>(rec) & 15))
+        return AQUA_ERR_INVALID;
+    if (n == 0)
+        return AQUA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (dims == 3)
+        k_node_records<3><<<blocks_for(n, 256), 256, 0, s>>>(
+            n, r, u, rho, imove, normal, reinterpret_cast<float4*>(rec));
+    else
+        k_node_records<2><<<blocks_for(n, 256), 256, 0, s>>>(
+            n, r, u, rho, imove, normal, reinterpret_cast<float4*>(rec));
+    return last_error();
+}
+
+aqua_status
+aqua_gnn_edge_features_rec(uint32_t E, int32_t dims, const uint32_t* recv,
+                           const uint32_t* send, const float* rec,
+                           const float* scales, uint16_t* out, void* stream)
+{
+    if ((dims != 2 && dims != 3) || !recv || !send || !rec || !scales ||
+        !out || (reinterpret_cast<uintptr_t>(rec) & 15))
+        return AQUA_ERR_INVALID;
+    if (E == 0)
+        return AQUA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const float4* r4 = reinterpret_cast<const float4*>(rec);
+    if (dims == 3)
+        k_edge_features_rec<3><<<blocks_for(E, 256), 256, 0, s>>>(
+            E, recv, send, r4, scales, out);
+    else
+        k_edge_features_rec<2><<<blocks_for(E, 256), 256, 0, s>>>(
+            E, recv, send, r4, scales, out);
     return last_error();
 }
 

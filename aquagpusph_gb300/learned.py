@@ -51,6 +51,9 @@ FUSE_EDGE_MLP = True
 # ... and sums its output into the receivers on chip as well (no E x 64
 # intermediate) when True
 FUSE_EDGE_SUM = True
+# edge features read packed per-node records (aqua_gnn_node_records) when
+# True, the separate node arrays otherwise; the features are the same
+EDGE_RECORDS = True
 
 _vp = C.c_void_p
 
@@ -89,6 +92,8 @@ SIGNATURES = {
                                _vp, _u32, _u32, _vp],
     "aqua_gnn_edge_features": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                _vp, _vp, _vp],
+    "aqua_gnn_node_records": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "aqua_gnn_edge_features_rec": [_u32, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
     "aqua_gnn_linear_fwd": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32,
                             _vp, _u32, _i32, _vp],
     "aqua_gnn_linear_fwd_tc": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _vp,
@@ -205,6 +210,11 @@ class Graph:
         _chk("aqua_gnn_neighbours", L.aqua_gnn_neighbours(
             nn, dims, _p(self.rs), _p(self.keys), ncell, _p(cstart), _p(cend),
             radius, _p(deg), _vp(0), _vp(0), _vp(0), s))
+        # 32-bit edge offsets (the kernels take E < 2^31)
+        total = int(deg.sum(dtype=torch.int64).item()) if nn else 0
+        if total >= 2 ** 31:
+            raise ValueError(f"{total} edges: the graph needs E < 2^31 "
+                             "(a smaller radius)")
         self.offsets = torch.empty(nn + 1, dtype=torch.int32, device=dev)
         scr = torch.empty(nn // 4096 + 4, dtype=torch.int32, device=dev)
         _chk("aqua_gnn_exclusive_scan", L.aqua_gnn_exclusive_scan(
@@ -461,9 +471,19 @@ class Network:
         s = self.s
         c = {}
         E0 = self._buf((max(E, 1), FEAT), torch.bfloat16)
-        _chk("aqua_gnn_edge_features", L.aqua_gnn_edge_features(
-            E, dims, _p(g.receivers), _p(g.senders), _p(x.r), _p(x.u), _p(x.rho),
-            _p(x.imove), _p(x.normal), _p(m.scales), _p(E0), s))
+        if EDGE_RECORDS:
+            rec = self._buf((max(n, 1), 12 if dims == 3 else 8), torch.float32)
+            _chk("aqua_gnn_node_records", L.aqua_gnn_node_records(
+                n, dims, _p(x.r), _p(x.u), _p(x.rho), _p(x.imove),
+                _p(x.normal), _p(rec), s))
+            _chk("aqua_gnn_edge_features_rec", L.aqua_gnn_edge_features_rec(
+                E, dims, _p(g.receivers), _p(g.senders), _p(rec), _p(m.scales),
+                _p(E0), s))
+            del rec
+        else:
+            _chk("aqua_gnn_edge_features", L.aqua_gnn_edge_features(
+                E, dims, _p(g.receivers), _p(g.senders), _p(x.r), _p(x.u),
+                _p(x.rho), _p(x.imove), _p(x.normal), _p(m.scales), _p(E0), s))
         c["E0"] = E0
         fused = self.fused and not train
         summed = self.fused_sum and not train

@@ -103,6 +103,20 @@ aqua_status aqua_gnn_edge_features(uint32_t n_edges, int32_t dims,
                                    const int32_t* imove, const float* normal,
                                    const float* scales, uint16_t* out,
                                    void* stream);
+/* The same edge features from packed node records: rec (16-byte aligned,
+ * AQUA_GNN_RECORD_FLOATS(dims) floats per node) is written by
+ * aqua_gnn_node_records from the node-ordered r, u, rho, imove, normal;
+ * the features are bit-identical to aqua_gnn_edge_features'. */
+#define AQUA_GNN_RECORD_FLOATS(dims) ((dims) == 3 ? 12 : 8)
+aqua_status aqua_gnn_node_records(uint32_t n, int32_t dims, const float* r,
+                                  const float* u, const float* rho,
+                                  const int32_t* imove, const float* normal,
+                                  float* rec, void* stream);
+aqua_status aqua_gnn_edge_features_rec(uint32_t n_edges, int32_t dims,
+                                       const uint32_t* receivers,
+                                       const uint32_t* senders,
+                                       const float* rec, const float* scales,
+                                       uint16_t* out, void* stream);
 
 /* ---- dense layers (tensor cores, bf16 x bf16 -> f32) ------------------- */
 

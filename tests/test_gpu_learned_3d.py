@@ -205,3 +205,49 @@ def test_field_runner_accepts_and_rolls_back(torch):
         assert st["n_edges"] > 0
         run.close()
         sv.close()
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_edge_features_from_records_equal_the_field_form(torch, dims):
+    """aqua_gnn_edge_features_rec on the packed node records writes the same
+    bits as aqua_gnn_edge_features on the separate node arrays."""
+    from aquagpusph_gb300 import learned as Lm
+    from aquagpusph_gb300.solver import Solver
+    if dims == 3:
+        c = small_3d()
+        b = cases.pack([c])
+    else:
+        b = cases.sloshing_batch_2d(n_cases=3, seed=5, dx=0.02)
+        c = b.case
+    sv = Solver(c.params, capacity=c.N,
+                ihoc_capacity=(len(b.offsets) - 1) * c.params.max_cells())
+    sv.set_batch(b)
+    sv.step(3, graph=True)
+    s0 = Lm.Snapshot.capture(sv, dims)
+    cid = Lm.case_ids(b)
+    g = Lm.Graph(sv, dims, s0["r"], s0["imove"], cid, s0.n,
+                 float(c.params.support * c.params.h))
+    x = Lm.Inputs(g, s0["r"], s0["u"], s0["rho"], s0["dudt"], s0["drhodt"],
+                  s0["imove"], s0["normal"])
+    L = Lm.lib()
+    sc = torch.tensor((float(c.params.h), 0.05, 0.5, 0.5, 5.0, 998.0),
+                      dtype=torch.float32, device="cuda")
+    E, n = g.n_edges, g.n_nodes
+    ref = torch.empty((E, 16), dtype=torch.bfloat16, device="cuda")
+    assert L.aqua_gnn_edge_features(E, dims, Lm._p(g.receivers),
+                                    Lm._p(g.senders), Lm._p(x.r), Lm._p(x.u),
+                                    Lm._p(x.rho), Lm._p(x.imove),
+                                    Lm._p(x.normal), Lm._p(sc), Lm._p(ref),
+                                    None) == 0
+    rec = torch.empty((n, 12 if dims == 3 else 8), dtype=torch.float32,
+                      device="cuda")
+    assert L.aqua_gnn_node_records(n, dims, Lm._p(x.r), Lm._p(x.u),
+                                   Lm._p(x.rho), Lm._p(x.imove),
+                                   Lm._p(x.normal), Lm._p(rec), None) == 0
+    got = torch.empty_like(ref)
+    assert L.aqua_gnn_edge_features_rec(E, dims, Lm._p(g.receivers),
+                                        Lm._p(g.senders), Lm._p(rec),
+                                        Lm._p(sc), Lm._p(got), None) == 0
+    torch.cuda.synchronize()
+    assert E > 0 and torch.equal(got.view(torch.int16), ref.view(torch.int16))
+    sv.close()
