@@ -220,7 +220,9 @@ k_linear_fwd_tc(uint32_t M, uint32_t K, const uint16_t* __restrict__ X,
 // to BF16 and writes the next layer's A operand into shared memory, exactly
 // the values the unfused layers store to and reload from global memory, so
 // the result is bit-identical to three aqua_gnn_linear_fwd_tc calls.  Only
-// the BF16 output of layer 3 is written.
+// the BF16 output of layer 3 is written.  A wait that times out sets *err;
+// the CTA finishes that tile (its outputs are then not to be trusted) and
+// stops.
 //
 // With SUM the layer-3 output never leaves the chip either: it is summed
 // into the receivers (aqua_gnn_segment_sum fused in).  Each CTA owns a
@@ -350,7 +352,8 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
     bool failed = false;
 
     // issue the MMAs of one layer (thread 0) and wait for them (everyone)
-    auto layer = [&](const uint8_t* sA, const uint8_t* sB, uint32_t K) -> bool {
+    bool tile_bad = false;
+    auto layer = [&](const uint8_t* sA, const uint8_t* sB, uint32_t K) {
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();
@@ -376,13 +379,14 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
                          "selp.u32 %0, 1, 0, p;\n}\n"
                          : "=r"(done) : "r"(smem_addr(&mbar)), "r"(phase));
         }
-        bool bad = !__all_sync(0xffffffffu, done);
+        // a time-out is recorded and acted on at the end of the tile (one
+        // CTA-wide vote per tile instead of one per layer)
+        const bool bad = !__all_sync(0xffffffffu, done);
         if (bad && lane == 0)
             atomicExch(err, 1);
-        bad = __syncthreads_or(bad);
+        tile_bad = tile_bad || bad;
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;\n");
-        return !bad;
     };
     // this thread's row of the accumulator and half of its columns
     const uint32_t row = (warp & 3u) * 32u + lane;
@@ -540,20 +544,11 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         // CTA's edges): it tells whether the tile's last run is complete
         if (SUM && tid == 0)
             ss->next_recv = ei_next;
-        if (!layer(sA1, sW1, K1)) {
-            failed = true;
-            break;
-        }
+        layer(sA1, sW1, K1);
         epilogue(0, act1, to_a1);
-        if (!layer(sA1, sW2, 64)) {
-            failed = true;
-            break;
-        }
+        layer(sA1, sW2, 64);
         epilogue(1, act2, to_a1);
-        if (!layer(sA1, sW3, 64)) {
-            failed = true;
-            break;
-        }
+        layer(sA1, sW3, 64);
         if constexpr (!SUM) {
             epilogue(2, act3, [&](int g, uint4 val) {
                 if (valid)
@@ -641,9 +636,9 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
             }
         }
         // the tile after next reuses this buffer; the next tile's MMAs
-        // reuse the accumulator
+        // reuse the accumulator; a time-out in any layer ends the CTA
         asm volatile("tcgen05.fence::before_thread_sync;\n");
-        __syncthreads();
+        failed = __syncthreads_or(tile_bad);
         ei_cur = ei_next;
         es_cur = es_next;
         cur = (cur + 1u) % kBufs;
