@@ -57,10 +57,15 @@ struct aqua_ctx
     uint32_t graph_n = 0, graph_cases = 0;
     int graph_motion = -1;
     // pinned staging areas of the small host -> device copies (case scalars,
-    // motions, offsets): one for aqua_set_state, one for aqua_set_cases, each
-    // reused once its event shows the copies that last read it executed
-    uint8_t* stage[2] = { nullptr, nullptr };
-    cudaEvent_t stage_ev[2] = { nullptr, nullptr };
+    // motions, offsets): a ring of kStageRing for aqua_set_state and one for
+    // aqua_set_cases; an area is reused once its event shows that the copies
+    // that last read it executed, which with a ring of four is almost never
+    // a wait (the host may run several calls ahead of the device)
+    static constexpr int kStageRing = 4;
+    uint8_t* stage[2][kStageRing] = {};
+    cudaEvent_t stage_ev[2][kStageRing] = {};
+    int stage_next[2] = { 0, 0 };  // the ring entry stage_begin hands out
+    int stage_cur[2] = { 0, 0 };   // the entry in use, for stage_done
     // stage boundary events (recorded when profiling is on): before the
     // link-list, before the gather, before the sweep, after the sweep, end
     static constexpr int kEvents = 5;
@@ -271,14 +276,18 @@ constexpr int kStageCases = 1;  // aqua_set_cases
 uint8_t*
 stage_begin(aqua_ctx* x, int slot)
 {
-    return cudaEventSynchronize(x->stage_ev[slot]) == cudaSuccess ? x->stage[slot]
-                                                                  : nullptr;
+    const int k = x->stage_next[slot];
+    x->stage_cur[slot] = k;
+    x->stage_next[slot] = (k + 1) % aqua_ctx::kStageRing;
+    return cudaEventSynchronize(x->stage_ev[slot][k]) == cudaSuccess
+               ? x->stage[slot][k]
+               : nullptr;
 }
 
 cudaError_t
 stage_done(aqua_ctx* x, int slot, cudaStream_t s)
 {
-    return cudaEventRecord(x->stage_ev[slot], s);
+    return cudaEventRecord(x->stage_ev[slot][x->stage_cur[slot]], s);
 }
 
 // Launches one step on `s` (the resident state advances from set[cur] to
@@ -492,15 +501,15 @@ aqua_create(const aqua_params* params, uint32_t capacity,
             delete x;
             return AQUA_ERR_CUDA;
         }
-    if (cudaMemset(x->pool, 0, x->pool_bytes) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&x->cap_stream, cudaStreamNonBlocking) !=
-            cudaSuccess ||
-        cudaMallocHost(&x->stage[0], kStageBytes) != cudaSuccess ||
-        cudaMallocHost(&x->stage[1], kStageBytes) != cudaSuccess ||
-        cudaEventCreateWithFlags(&x->stage_ev[0], cudaEventDisableTiming) !=
-            cudaSuccess ||
-        cudaEventCreateWithFlags(&x->stage_ev[1], cudaEventDisableTiming) !=
-            cudaSuccess) {
+    bool ok = cudaMemset(x->pool, 0, x->pool_bytes) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&x->cap_stream, cudaStreamNonBlocking) ==
+                  cudaSuccess;
+    for (int k = 0; ok && k < 2; k++)
+        for (int q = 0; ok && q < aqua_ctx::kStageRing; q++)
+            ok = cudaMallocHost(&x->stage[k][q], kStageBytes) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&x->stage_ev[k][q],
+                                          cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
         aqua_destroy(x);
         return AQUA_ERR_CUDA;
     }
@@ -519,14 +528,15 @@ aqua_destroy(aqua_ctx* x)
     for (int k = 0; k < aqua_ctx::kEvents; k++)
         if (x->ev[k])
             cudaEventDestroy(x->ev[k]);
-    for (int k = 0; k < 2; k++) {
-        if (x->stage_ev[k]) {
-            cudaEventSynchronize(x->stage_ev[k]);  // no copy still reads it
-            cudaEventDestroy(x->stage_ev[k]);
+    for (int k = 0; k < 2; k++)
+        for (int q = 0; q < aqua_ctx::kStageRing; q++) {
+            if (x->stage_ev[k][q]) {
+                cudaEventSynchronize(x->stage_ev[k][q]);  // no copy still reads it
+                cudaEventDestroy(x->stage_ev[k][q]);
+            }
+            if (x->stage[k][q])
+                cudaFreeHost(x->stage[k][q]);
         }
-        if (x->stage[k])
-            cudaFreeHost(x->stage[k]);
-    }
     if (x->pool)
         cudaFree(x->pool);
     delete x;
