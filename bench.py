@@ -414,14 +414,21 @@ def run_ours(args):
     # host jitter does not dominate short steps
     e2e_steps = max(args.steps, int(math.ceil(200.0 / max(ms_step, 1e-3))))
     e2e_steps = 2 * max(1, min(e2e_steps, 200) // 2)
-    ctxs = ((sv, sid), (sv2, sid2))
+    ctxs = ((sv, sid, stream), (sv2, sid2, stream2))
+    # the steps of the two contexts run one after the other (each waits for
+    # the other's previous step), so that they do not share the SMs and the
+    # L2; each context's copies overlap the other's step
+    step_done = (torch.cuda.Event(), torch.cuda.Event())
 
     def e2e_round_trip(k):
-        s_, sid_ = ctxs[k % 2]
+        s_, sid_, st_ = ctxs[k % 2]
         s_.set_state_raw(c.N, addr_in, True, c.t, c.dt, c.iter, stream=sid_)
         if batch:
             s_.set_cases(batch, stream=sid_)
+        if k > 0:
+            st_.wait_event(step_done[(k - 1) % 2])
         s_.step(1, graph=True, stream=sid_)
+        step_done[k % 2].record(st_)
         s_.get_state_raw(addr_out[k % 2], True, stream=sid_)
 
     # one untimed round trip per context (the stage profiling above dropped
