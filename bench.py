@@ -410,10 +410,11 @@ def run_ours(args):
     addr_out = [{k: t.data_ptr() for k, t in o.items()} for o in outs]
     h2d = sum(t.numel() for t in host.values())
     d2h = sum(t.numel() for t in outs[0].values())
-    # about 0.2 s of device work (at least K steps, at most 200), so that
-    # host jitter does not dominate short steps
-    e2e_steps = max(args.steps, int(math.ceil(200.0 / max(ms_step, 1e-3))))
-    e2e_steps = 2 * max(1, min(e2e_steps, 200) // 2)
+    # about 0.5 s of device work (at least K steps, at most 400), so that
+    # host jitter and the loop's first upload and last download (which
+    # nothing hides) weigh little
+    e2e_steps = max(args.steps, int(math.ceil(500.0 / max(ms_step, 1e-3))))
+    e2e_steps = 2 * max(1, min(e2e_steps, 400) // 2)
     ctxs = ((sv, sid, stream), (sv2, sid2, stream2))
     # the steps of the two contexts run one after the other (each waits for
     # the other's previous step), so that they do not share the SMs and the
