@@ -62,3 +62,17 @@ def test_single_rank_is_identity():
     import bench
     assert bench.max_over_ranks(3.5, 1) == 3.5
     assert bench.job_throughput(1, 10, 4, 2.0) == 20.0
+
+
+def test_workload_table_is_shared_by_both_arms():
+    """Every workload the bench accepts has one description and particle
+    count, which the CPU sample of the reference arm names too; the learned
+    workloads extend their plain workload's description."""
+    import bench
+    for name in ("c0", "c1", "c1s", "c1m", "c2", "c4"):
+        desc = bench.workload_desc(name)
+        d, n = bench.WORKLOADS[name]
+        assert desc == f"{d}: N={n}"
+    assert bench.workload_desc("c3").startswith(bench.workload_desc("c2"))
+    assert bench.workload_desc("c5").startswith(bench.workload_desc("c4"))
+    assert "whole field" in bench.workload_desc("c5")
