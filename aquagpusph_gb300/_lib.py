@@ -146,6 +146,8 @@ SIGNATURES = [
     ("aqua_radix_sort", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_uint32, C.c_uint32,
                                   C.c_void_p]),
+    ("aqua_set_rate_sample", C.c_int, [C.c_void_p, C.c_float, C.c_uint32]),
+    ("aqua_debug_fake_timeouts", C.c_int, [C.c_int]),
     ("aqua_radix_sort_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_uint32, C.c_uint32, C.c_void_p]),
     ("aqua_set_profiling", C.c_int, [C.c_void_p, C.c_int]),

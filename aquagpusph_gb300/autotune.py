@@ -31,6 +31,10 @@ VARIANTS = ((0, 128, 128, 24), (1, 64, 128, 24), (2, 64, 64, 24),
 # resident warps per SM tried for each variant (blocks = warps * 32 / threads)
 WARPS_PER_SM = (8, 12, 16, 20, 24, 28, 32, 36)
 MAX_BLOCKS_PER_SM = 32
+# the clustered sweep of the fast 3-D build (BIe walls, midpoint scheme):
+# (variant, threads per block, blocks per SM tried); 15 and 17 hold at most
+# 2 blocks per SM, 16 at most 3 (shared memory, registers)
+CLUSTERED = ((15, 256, (1, 2)), (16, 256, (1, 2, 3)), (17, 384, (1, 2)))
 
 
 def cache_path() -> str:
@@ -81,13 +85,25 @@ def _save(d):
         pass
 
 
-def candidates():
+def clustered_applies(solver, fast: bool) -> bool:
+    """The clustered sweep runs for the fast build in 3-D with BIe walls and
+    the midpoint scheme."""
+    p = solver.params
+    return bool(fast and p.dims == 3 and getattr(p, "boundary", 0) == 0 and
+                getattr(p, "scheme", 0) == 0)
+
+
+def candidates(clustered: bool = False):
     for v, threads, queue, most in VARIANTS:
         for w in WARPS_PER_SM:
             if w > most:
                 continue
             b = w * 32 // threads
             if b * threads == w * 32 and 1 <= b <= MAX_BLOCKS_PER_SM:
+                yield v, b
+    if clustered:
+        for v, threads, blocks in CLUSTERED:
+            for b in blocks:
                 yield v, b
 
 
@@ -103,7 +119,7 @@ def autotune(solver, fast: bool, steps: int = 3, use_cache: bool = True,
         solver.set_tuning(v, b)
         return dict(cache[key], cached=True)
     results = []
-    for v, b in candidates():
+    for v, b in candidates(clustered_applies(solver, fast)):
         try:
             solver.set_tuning(v, b)
         except _lib.AquaError:
@@ -119,9 +135,10 @@ def autotune(solver, fast: bool, steps: int = 3, use_cache: bool = True,
     results.sort()
     best_dt, v, b = results[0]
     solver.set_tuning(v, b)
+    threads = dict((x[0], x[1]) for x in VARIANTS + CLUSTERED)
     entry = {"variant": v, "blocks_per_sm": b,
-             "threads": dict((x[0], x[1]) for x in VARIANTS)[v],
-             "queue": dict((x[0], x[2]) for x in VARIANTS)[v],
+             "threads": threads[v],
+             "queue": dict((x[0], x[2]) for x in VARIANTS).get(v, 0),
              "ms_per_step": 1e3 * best_dt,
              "candidates": [[round(1e3 * d, 4), vv, bb] for d, vv, bb in results]}
     if use_cache:

@@ -16,6 +16,13 @@
 
 using namespace aqua;
 
+namespace aqua {
+// test-only switch of aqua_debug_fake_timeouts(): read when a step or a
+// tensor-core kernel is enqueued (graphs keep the value they were captured
+// with)
+int g_debug_fake_timeout = 0;
+}  // namespace aqua
+
 namespace {
 constexpr uint32_t kMaxCases = 4096;
 }
@@ -47,7 +54,8 @@ struct aqua_ctx
     int extras = 0;
     int fast = 0;              // 1: -use_fast_math step kernels
     unsigned sweep_grid = 0;   // persistent sweep blocks
-    int sweep_variant = 9;     // launch shape of the sweep (aqua_set_tuning)
+    int sweep_variant = kSweepClusteredDefault;  // launch shape of the sweep
+                                                 // (aqua_set_tuning)
     int sms = 1;
     void* pool = nullptr;
     size_t pool_bytes = 0;
@@ -236,6 +244,13 @@ layout(aqua_ctx* x, char* base)
     b.grad_w_bi = cv.take<float>((size_t)n * VS);
     b.div_u_bi = cv.take<float>(n);
     b.shepard = cv.take<float>(n);
+    b.rec0 = cv.take<float4>(n);
+    b.rec1 = cv.take<float4>(n);
+    b.cell_mark = cv.take<uint8_t>(x->ncap);
+    b.work = cv.take<uint2>(n);
+    b.wcl = cv.take<uint4>(n);
+    b.clu = cv.take<uint2>(n);
+    b.cperm = cv.take<uint32_t>(n);
     x->sc = cv.take<DevScalars>(1);
     x->sc_aux = cv.take<DevScalars>(1);
     x->cs = cv.take<CaseScalars>(kMaxCases);
@@ -290,6 +305,16 @@ stage_done(aqua_ctx* x, int slot, cudaStream_t s)
     return cudaEventRecord(x->stage_ev[slot][x->stage_cur[slot]], s);
 }
 
+// The clustered sweep runs for the fast build in 3-D with BIe walls and the
+// midpoint scheme when the chosen variant is a clustered one
+bool
+sweep_clustered(const aqua_ctx* x)
+{
+    return x->fast && x->dims == 3 && x->sweep_variant >= kSweepClustered &&
+           x->consts.boundary == AQUA_BOUNDARY_BIE &&
+           x->consts.scheme == AQUA_SCHEME_MIDPOINT;
+}
+
 // Launches one step on `s` (the resident state advances from set[cur] to
 // set[cur ^ 1]; the caller flips cur).
 aqua_status
@@ -302,7 +327,8 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[0], s, cudaEventRecordExternal));
     AQ_CUDA(launch_begin(x->sc, x->cs, x->n_cases, b.cells, b.wall_range,
-                         x->ncap, N, s));
+                         x->consts.sample_on ? b.cell_mark : nullptr, x->ncap,
+                         N, s));
     if (x->dims == 3) {
         AQ_CUDA(launch_minmax<3>(x->consts, S.r, S.imove, S.cid, N, x->cs,
                                  x->sc, s));
@@ -331,6 +357,10 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     a.cm = x->cm;
     a.n_cases = x->n_cases;
     a.extras = x->extras;
+    const bool clustered = sweep_clustered(x);
+    a.clustered = clustered ? 1 : 0;
+    Consts cst = x->consts;
+    cst.debug_fake_timeout = g_debug_fake_timeout ? 1u : 0u;
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[1], s, cudaEventRecordExternal));
     if (x->dims == 3)
@@ -345,12 +375,20 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     }
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[2], s, cudaEventRecordExternal));
-    if (x->dims == 3)
-        AQ_CUDA(launch_sweep<3>(x->fast, x->consts, a, x->sweep_grid,
-                                x->sweep_variant, s));
-    else
-        AQ_CUDA(launch_sweep<2>(x->fast, x->consts, a, x->sweep_grid,
-                                x->sweep_variant, s));
+    if (clustered) {
+        AQ_CUDA(fast::launch_sweep_cl(cst, a, x->sweep_grid, x->sweep_variant,
+                                      (unsigned)x->sms, s));
+    } else {
+        // a clustered choice where the clustered sweep does not apply falls
+        // back to the direct sweep's untuned shape
+        const bool cl_pick = x->sweep_variant >= kSweepClustered;
+        const int v = cl_pick ? 9 : x->sweep_variant;
+        const unsigned g = cl_pick ? (unsigned)x->sms * 14u : x->sweep_grid;
+        if (x->dims == 3)
+            AQ_CUDA(launch_sweep<3>(x->fast, cst, a, g, v, s));
+        else
+            AQ_CUDA(launch_sweep<2>(x->fast, cst, a, g, v, s));
+    }
     if (x->profiling)
         AQ_CUDA(cudaEventRecordWithFlags(x->ev[3], s, cudaEventRecordExternal));
     AQ_CUDA(launch_finalize(x->sc, x->cs, x->cm, x->n_cases, s));
@@ -464,7 +502,7 @@ aqua_create(const aqua_params* params, uint32_t capacity,
     if (!out || capacity == 0)
         return AQUA_ERR_INVALID;
     *out = nullptr;
-    Consts c;
+    Consts c{};
     AQ_TRY(build_consts(params, c));
     aqua_ctx* x = new (std::nothrow) aqua_ctx();
     if (!x)
@@ -486,8 +524,14 @@ aqua_create(const aqua_params* params, uint32_t capacity,
         return AQUA_ERR_CUDA;
     }
     x->sms = sms > 0 ? sms : 1;
-    // untuned default: the direct sweep with prefetch, 28 warps per SM
-    x->sweep_grid = (unsigned)x->sms * 14u;
+    // untuned default: the clustered sweep (fast 3-D BIe midpoint) with 3
+    // blocks of 8 warps per SM; elsewhere the direct sweep with prefetch at
+    // 28 warps per SM (see enqueue_step)
+    x->sweep_grid = (unsigned)x->sms * kSweepClusteredBlocks;
+    if (fast::prepare_sweep_cl() != cudaSuccess) {
+        delete x;
+        return AQUA_ERR_CUDA;
+    }
     x->pool_bytes = layout(x, nullptr);
     if (cudaMalloc(&x->pool, x->pool_bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -548,8 +592,12 @@ aqua_set_params(aqua_ctx* x, const aqua_params* params)
 {
     if (!x || !params || params->dims != x->dims)
         return AQUA_ERR_INVALID;
-    Consts c;
+    Consts c{};
     AQ_TRY(build_consts(params, c));
+    // the rate sample is a setting of the context, not of the parameters
+    c.sample_on = x->consts.sample_on;
+    c.sample_thr = x->consts.sample_thr;
+    c.sample_seed = x->consts.sample_seed;
     x->consts = c;
     drop_graphs(x);
     return AQUA_OK;
@@ -970,7 +1018,8 @@ aqua_linklist(aqua_ctx* x, const float* r_in, uint32_t N, uint32_t* icell,
     DevScalars hs;
     std::memset(&hs, 0, sizeof(hs));
     AQ_CUDA(cudaMemcpyAsync(x->sc_aux, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
-    AQ_CUDA(launch_begin(x->sc_aux, x->cs_aux, 1, b.cells, b.wall_range, 0, N, s));
+    AQ_CUDA(launch_begin(x->sc_aux, x->cs_aux, 1, b.cells, b.wall_range,
+                         nullptr, 0, N, s));
     if (x->dims == 3) {
         AQ_CUDA(launch_minmax<3>(x->consts, r_in, nullptr, nullptr, N, x->cs_aux,
                                  x->sc_aux, s));
@@ -1036,14 +1085,37 @@ aqua_stage_times(aqua_ctx* x, float* ms, uint32_t n)
     return AQUA_OK;
 }
 
+aqua_status
+aqua_set_rate_sample(aqua_ctx* x, float fraction, uint32_t seed)
+{
+    if (!x || !(fraction > 0.f))
+        return AQUA_ERR_INVALID;
+    if (fraction >= 1.f) {
+        x->consts.sample_on = 0;
+    } else {
+        x->consts.sample_on = 1;
+        x->consts.sample_thr = (uint32_t)((double)fraction * 4294967296.0);
+        x->consts.sample_seed = seed;
+    }
+    drop_graphs(x);
+    return AQUA_OK;
+}
+
+aqua_status
+aqua_debug_fake_timeouts(int on)
+{
+    g_debug_fake_timeout = on ? 1 : 0;
+    return AQUA_OK;
+}
+
 uint32_t
 aqua_launches_per_step(aqua_ctx* x)
 {
     if (!x)
         return 0;
     // begin, minmax, ncells, icell+hist, (passes - 1) hist,
-    // passes x (scan, scatter), gather, [BI walls,] chunks, sweep, finalize
-    // [, motion]
+    // passes x (scan, scatter), gather, [BI walls,] chunks or clusters,
+    // sweep, finalize [, motion]
     return 4u + (x->passes - 1u) + 2u * x->passes + 4u +
            (x->consts.boundary == AQUA_BOUNDARY_BI ? 1u : 0u) +
            (x->has_motion ? 1u : 0u);

@@ -18,6 +18,10 @@ namespace aqua {
 
 constexpr int kMaxSets = 16;
 
+// test-only switch of aqua_debug_fake_timeouts() (api.cu): bounded waits
+// that completed report a time-out
+extern int g_debug_fake_timeout;
+
 // Error word bits written by kernels (read back by aqua_check)
 enum : uint32_t
 {
@@ -50,7 +54,28 @@ struct Consts
     float inv_H;        // 1 / H
     float w_conw;       // W factor of the Wendland kernel * CONW
     float f_conf;       // F factor * CONF
+    // test-only: a bounded wait that completed is reported as timed out
+    // (AQUA_ERR_TIMEOUT), so the error path runs with nothing in flight
+    uint32_t debug_fake_timeout;
+    // rate sample (aqua_set_rate_sample): the clustered sweep runs only the
+    // cells whose key hashes below sample_thr, and every cell around a probe
+    uint32_t sample_on;
+    uint32_t sample_thr;
+    uint32_t sample_seed;
 };
+
+// 32-bit hash of a cell key for the rate sample (host and device)
+__host__ __device__ inline uint32_t
+sample_hash(uint32_t key, uint32_t seed)
+{
+    uint32_t h = key * 0x9E3779B1u ^ (seed * 0x85EBCA77u + 0x165667B1u);
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
 
 // Device-side scalars of one case of the resident state (a batch holds
 // n_cases independent cases, each with its own link-list and time step)
@@ -89,7 +114,8 @@ struct DevScalars
     uint32_t n_chunks;    // cell-aligned sweep chunks of this step
     uint32_t chunk_next;  // next chunk to hand out (work counter)
     uint32_t total_cells; // cells of all cases
-    uint32_t pad[4];
+    uint32_t n_clusters;  // particle clusters of the clustered sweep
+    uint32_t pad[3];
 };
 
 // One set of the per-particle Variables (reference layout)
@@ -144,6 +170,21 @@ struct StepBufs
     float* grad_w_bi;
     float* div_u_bi;
     float* shepard;
+    // clustered sweep (fast build, 3-D): per sorted particle two 16-byte
+    // neighbour records, rec0 = (x, y, z, w) with w = m/rho (fluid), -m
+    // (boundary element, its area) or 0 (no neighbour sums), rec1 = (u, p)
+    // (fluid) or (normal, u.normal) (boundary element); the cells holding
+    // particles as (key, first sorted index) in `work`, their cluster
+    // ranges in `wcl` (first, end, first cluster, clusters); clusters of
+    // <= 8 particles of one cell octant as (first position in cperm,
+    // count); cperm = sorted indices in cluster order
+    float4* rec0;
+    float4* rec1;
+    uint8_t* cell_mark;    // rate sample: cells around a probe (ncap)
+    uint2* work;
+    uint4* wcl;
+    uint2* clu;
+    uint32_t* cperm;
 };
 
 }  // namespace aqua

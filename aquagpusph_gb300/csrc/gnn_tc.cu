@@ -19,6 +19,11 @@
 
 #include "aqua_learned.h"
 
+namespace aqua {
+// test-only switch of aqua_debug_fake_timeouts() (api.cu)
+extern int g_debug_fake_timeout;
+}  // namespace aqua
+
 namespace {
 
 constexpr int kTcThreads = 128;
@@ -93,7 +98,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 k_linear_fwd_tc(uint32_t M, uint32_t K, const uint16_t* __restrict__ X,
                 uint32_t ldx, const uint16_t* __restrict__ W,
                 const float* __restrict__ bias, float* Z, uint32_t ldz,
-                uint16_t* Y, uint32_t ldy, int act, int* err)
+                uint16_t* Y, uint32_t ldy, int act, int* err, uint32_t fake)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
@@ -151,7 +156,8 @@ k_linear_fwd_tc(uint32_t M, uint32_t K, const uint16_t* __restrict__ X,
                          "selp.u32 %0, 1, 0, p;\n}\n"
                          : "=r"(done) : "r"(smem_addr(&mbar)), "r"(phase));
         }
-        if (!__all_sync(0xffffffffu, done)) {
+        // `fake` (test switch): a wait that completed counts as timed out
+        if (!__all_sync(0xffffffffu, done) || fake) {
             failed = true;
             if (lane == 0)
                 atomicExch(err, 1);
@@ -297,6 +303,7 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
               const uint16_t* __restrict__ W2, const float* __restrict__ b2,
               const uint16_t* __restrict__ W3, const float* __restrict__ b3,
               int act1, int act2, int act3, uint16_t* Y, uint32_t ldy, int* err,
+              uint32_t fake,
               uint32_t n_nodes, const uint32_t* __restrict__ off, float scale,
               uint32_t col)
 {
@@ -381,7 +388,7 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
         }
         // a time-out is recorded and acted on at the end of the tile (one
         // CTA-wide vote per tile instead of one per layer)
-        const bool bad = !__all_sync(0xffffffffu, done);
+        const bool bad = !__all_sync(0xffffffffu, done) || fake != 0u;
         if (bad && lane == 0)
             atomicExch(err, 1);
         tile_bad = tile_bad || bad;
@@ -751,7 +758,7 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
         k_edge_mlp_tc<144, true, false>
             <<<grid, kEdgeThreads, edge_mlp_smem<144>(), s>>>(
                 E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
-                act1, act2, act3, Y, ldy, err, 0u, nullptr, 0.f, 0u);
+                act1, act2, act3, Y, ldy, err, (uint32_t)aqua::g_debug_fake_timeout, 0u, nullptr, 0.f, 0u);
     } else {
         // 52 KB: three CTAs per SM (registers; 192 TMEM columns)
         const uint32_t cap = (uint32_t)sms * edge_ctas_per_sm<false>();
@@ -759,7 +766,7 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
         k_edge_mlp_tc<16, false, false>
             <<<grid, kEdgeThreads, edge_mlp_smem<16>(), s>>>(
                 E, X, ldx, nullptr, nullptr, nullptr, 0, nullptr, W1, b1, W2,
-                b2, W3, b3, act1, act2, act3, Y, ldy, err, 0u, nullptr, 0.f, 0u);
+                b2, W3, b3, act1, act2, act3, Y, ldy, err, (uint32_t)aqua::g_debug_fake_timeout, 0u, nullptr, 0.f, 0u);
     }
     return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
 }
@@ -801,12 +808,12 @@ aqua_gnn_edge_mlp_sum_tc(uint32_t n_nodes, uint32_t E, uint32_t K1,
         k_edge_mlp_tc<144, true, true>
             <<<grid, kEdgeThreads, edge_mlp_smem<144>(), s>>>(
                 E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
-                act1, act2, act3, out, ld, err, n_nodes, offsets, scale, col);
+                act1, act2, act3, out, ld, err, (uint32_t)aqua::g_debug_fake_timeout, n_nodes, offsets, scale, col);
     else
         k_edge_mlp_tc<16, false, true>
             <<<grid, kEdgeThreads, edge_mlp_smem<16>(), s>>>(
                 E, X, ldx, recv, nullptr, nullptr, 0, nullptr, W1, b1, W2, b2,
-                W3, b3, act1, act2, act3, out, ld, err, n_nodes, offsets, scale,
+                W3, b3, act1, act2, act3, out, ld, err, (uint32_t)aqua::g_debug_fake_timeout, n_nodes, offsets, scale,
                 col);
     return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
 }
@@ -849,6 +856,6 @@ aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N, const uint16_t* X,
     const uint32_t tiles = (M + kTcRows - 1) / kTcRows;
     const uint32_t grid = tiles < (uint32_t)sms * 8u ? tiles : (uint32_t)sms * 8u;
     k_linear_fwd_tc<64><<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
-        M, K, X, ldx, W, b, Z, ldz, Y, ldy, act, err);
+        M, K, X, ldx, W, b, Z, ldz, Y, ldy, act, err, (uint32_t)aqua::g_debug_fake_timeout);
     return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
 }

@@ -17,10 +17,18 @@ constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block
 // prefetched by asynchronous copies: 7 = 64 threads, 8 = 128 threads;
 // those with the register budget of 28 resident warps per SM (9 = 64,
 // 10 = 128 threads), 32 (11, 12) or 36 (13, 14)
-constexpr int kSweepVariants = 15;
+// the clustered sweep of the fast 3-D build (BIe walls, midpoint scheme):
+// 15 = 8 warps per block for 2 blocks per SM, 16 = 8 warps for 3 blocks,
+// 17 = 12 warps for 2 blocks; each stages 2,048 neighbour records per pass
+constexpr int kSweepClustered = 15;
+constexpr int kSweepVariants = 18;
+constexpr int kSweepClusteredDefault = 16;
+constexpr unsigned kSweepClusteredBlocks = 3;
 inline int
 sweep_variant_threads(int v)
 {
+    if (v >= kSweepClustered)
+        return v == kSweepClustered + 2 ? 384 : 256;
     return (v == 0 || (v >= 6 && v % 2 == 0)) ? 128 : 64;
 }
 
@@ -82,8 +90,8 @@ struct Vec<2>
 // link-list / sort launchers (linklist.cu).  `cid` (case of each particle)
 // may be NULL: every particle then belongs to case 0.
 cudaError_t launch_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases,
-                         uint2* cells, uint2* wall_range, uint32_t ncap,
-                         uint32_t N, cudaStream_t s);
+                         uint2* cells, uint2* wall_range, uint8_t* cell_mark,
+                         uint32_t ncap, uint32_t N, cudaStream_t s);
 template<int D>
 cudaError_t launch_minmax(const Consts& c, const float* r, const int32_t* imove,
                           const uint32_t* cid, uint32_t N, CaseScalars* cs,
@@ -125,6 +133,8 @@ struct StepArgs
     const CaseMotion* cm;   // per-case prescribed motion (n_cases)
     uint32_t n_cases;
     int extras;        // write the intermediate operators
+    int clustered;     // the gather writes rec0/rec1 and the cell list for
+                       // the clustered sweep instead of posq/velq/pmq
 };
 // gather / sweep of the step in the exact (IEEE, no FMA) or fast
 // (-use_fast_math) compilation
@@ -178,6 +188,11 @@ cudaError_t launch_sweep_impl(const Consts& c, const StepArgs& a, unsigned grid,
                               int variant, cudaStream_t s);
 }  // namespace exact
 namespace fast {
+// clustered sweep: the cluster list then the sweep (variant >= kSweepClustered)
+cudaError_t launch_sweep_cl(const Consts& c, const StepArgs& a, unsigned grid,
+                            int variant, unsigned sms, cudaStream_t s);
+// sets the kernels' dynamic shared memory limit (once, before any capture)
+cudaError_t prepare_sweep_cl();
 template<int D>
 cudaError_t launch_bi_walls_impl(const Consts& c, const StepArgs& a, cudaStream_t s);
 template<int D>

@@ -86,7 +86,7 @@ domain_position(const Consts& c, const float* r, const int32_t* imove,
 // Resets the per-step scalars of every case and clears the cell table.
 __global__ void
 k_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases, uint2* cells,
-        uint2* wall_range, uint32_t ncap, uint32_t N)
+        uint2* wall_range, uint8_t* cell_mark, uint32_t ncap, uint32_t N)
 {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     for (uint32_t k = tid; k < n_cases; k += gridDim.x * blockDim.x) {
@@ -99,12 +99,15 @@ k_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases, uint2* cells,
     if (tid == 0) {
         sc->n_chunks = 0;
         sc->chunk_next = 0;
+        sc->n_clusters = 0;
     }
     if (sc->err)
         return;
     for (uint32_t c = tid; c < ncap; c += gridDim.x * blockDim.x) {
         cells[c] = make_uint2(N, N);
         wall_range[c] = make_uint2(0xffffffffu, 0u);
+        if (cell_mark)
+            cell_mark[c] = 0;
     }
 }
 
@@ -529,10 +532,12 @@ grid_for(uint32_t n, unsigned threads)
 
 cudaError_t
 launch_begin(DevScalars* sc, CaseScalars* cs, uint32_t n_cases, uint2* cells,
-             uint2* wall_range, uint32_t ncap, uint32_t N, cudaStream_t s)
+             uint2* wall_range, uint8_t* cell_mark, uint32_t ncap, uint32_t N,
+             cudaStream_t s)
 {
     const unsigned g = min(grid_for(max(ncap, n_cases), 256), 152u * 8u);
-    k_begin<<<max(g, 1u), 256, 0, s>>>(sc, cs, n_cases, cells, wall_range, ncap, N);
+    k_begin<<<max(g, 1u), 256, 0, s>>>(sc, cs, n_cases, cells, wall_range,
+                                        cell_mark, ncap, N);
     return cudaGetLastError();
 }
 

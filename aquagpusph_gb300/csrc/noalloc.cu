@@ -6,20 +6,31 @@
 // up front by that runtime (as the reference's Variables registry does),
 // code running while a stream is being captured into a CUDA graph, or a
 // process that works under a fixed device-memory budget.  Such callers get
-// a sort that needs no context: its scratch is the file-scope array below,
-// which exists on every GPU that loads the library, from load until exit.
+// a sort that needs no context: its scratch is the file-scope array below.
 //
 // Limits and sharing:
 //   - at most AQUA_NOALLOC_SORT_MAX_KEYS keys per call (larger sizes are
 //     rejected with AQUA_ERR_CAPACITY before anything is launched);
-//   - all calls on a device share the one array and it keeps the contents
-//     of the last call: calls whose work overlaps on the GPU (different
-//     streams without ordering between them) race and give wrong results;
-//   - the first call on a device looks the array's device address up
-//     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture.
+//   - all calls in one CUDA context share the one array and it keeps the
+//     contents of the last call: calls whose work overlaps on the GPU
+//     (different streams without ordering between them) race and give wrong
+//     results;
+//   - the array belongs to the library's module in a CUDA context, so its
+//     device address differs between contexts (a driver-API host's own
+//     context, the primary context re-created after cudaDeviceReset).  The
+//     address is looked up (cudaGetSymbolAddress) the first time a context
+//     calls, and again whenever the calling thread's current context is one
+//     not seen before; contexts are told apart by their unique id
+//     (cuCtxGetId), never by device index or handle value;
+//   - that first call in a context is also where the array's memory is
+//     committed (CUDA loads modules lazily), so under a fixed budget it is
+//     the call that can fail; make it before any stream capture.  A call
+//     that would need the lookup while its stream is capturing returns
+//     AQUA_ERR_INVALID without launching anything.
 #include <cstdio>
 #include <mutex>
+
+#include <cuda.h>
 
 #include "aqua_internal.cuh"
 #include "kernels.cuh"
@@ -35,29 +46,93 @@ constexpr size_t kWords = 3ull * kMaxKeys + 256ull * kMaxBlocks + 256ull;
 
 static __device__ __align__(256) uint32_t g_sort_scratch[kWords];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-uint32_t* g_scratch[kMaxDevices] = {};
-
-// Device address of g_sort_scratch on the current device (looked up once)
-aqua_status
-scratch_for_current_device(uint32_t** out)
+// Scratch addresses per CUDA context, keyed by the context's unique id
+constexpr int kMaxContexts = 32;
+struct ScratchEntry
 {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    unsigned long long ctx_id;
+    uint32_t* ptr;
+};
+std::mutex g_mutex;
+ScratchEntry g_entries[kMaxContexts] = {};
+int g_n_entries = 0;
+int g_next_victim = 0;
+
+// Driver entry points for the current context and its id, fetched through
+// the runtime (the library does not link libcuda directly)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+bool
+driver_entry_points()
+{
+    if (g_ctx_get_current && g_ctx_get_id)
+        return true;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                         cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000,
+                                         cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess ||
+        !f1 || !f2)
+        return false;
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    return true;
+}
+
+// Device address of g_sort_scratch in the calling thread's current context
+// (looked up once per context; refused while `stream` is capturing)
+aqua_status
+scratch_for_current_context(cudaStream_t stream, uint32_t** out)
+{
+    // binds the device's primary context when no context is current yet
+    if (cudaFree(nullptr) != cudaSuccess)
         return AQUA_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            std::fprintf(stderr, "aqua_radix_sort_noalloc: cudaGetSymbolAddress "
-                                 "failed: %s\n", cudaGetErrorString(e));
-            return AQUA_ERR_CUDA;
-        }
-        g_scratch[dev] = static_cast<uint32_t*>(p);
+    if (!driver_entry_points()) {
+        std::fprintf(stderr, "aqua_radix_sort_noalloc: the driver entry points "
+                             "cuCtxGetCurrent / cuCtxGetId are unavailable\n");
+        return AQUA_ERR_CUDA;
     }
-    *out = g_scratch[dev];
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx ||
+        g_ctx_get_id(ctx, &id) != CUDA_SUCCESS)
+        return AQUA_ERR_CUDA;
+    for (int k = 0; k < g_n_entries; k++)
+        if (g_entries[k].ctx_id == id) {
+            *out = g_entries[k].ptr;
+            return AQUA_OK;
+        }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess ||
+        cap != cudaStreamCaptureStatusNone) {
+        std::fprintf(stderr, "aqua_radix_sort_noalloc: the first call in a CUDA "
+                             "context must come before any stream capture\n");
+        return AQUA_ERR_INVALID;
+    }
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        std::fprintf(stderr, "aqua_radix_sort_noalloc: cudaGetSymbolAddress "
+                             "failed: %s\n", cudaGetErrorString(e));
+        return AQUA_ERR_CUDA;
+    }
+    int slot = g_n_entries;
+    if (g_n_entries < kMaxContexts) {
+        g_n_entries++;
+    } else {
+        slot = g_next_victim;
+        g_next_victim = (g_next_victim + 1) % kMaxContexts;
+    }
+    g_entries[slot].ctx_id = id;
+    g_entries[slot].ptr = static_cast<uint32_t*>(p);
+    *out = g_entries[slot].ptr;
     return AQUA_OK;
 }
 
@@ -86,11 +161,11 @@ aqua_radix_sort_noalloc(uint32_t* keys, uint32_t* perm, uint32_t* inv_perm,
     }
     if (n == 0)
         return AQUA_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     uint32_t* base = nullptr;
-    const aqua_status st = scratch_for_current_device(&base);
+    const aqua_status st = scratch_for_current_context(s, &base);
     if (st != AQUA_OK)
         return st;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     // the caller's keys are one half of the key ping-pong (sorted in place)
     uint32_t* kbuf[2] = { keys, base };
     uint32_t* vbuf[2] = { base + kMaxKeys, base + 2ull * kMaxKeys };

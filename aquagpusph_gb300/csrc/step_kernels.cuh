@@ -259,8 +259,22 @@ k_gather(Consts c, StepArgs a)
     }
     const uint32_t o = a.perm[s];
     a.b.id_sorted[o] = s;
-    if (s == 0 || a.skeys[s - 1] != key)
+    const bool cell_start = s == 0 || a.skeys[s - 1] != key;
+    if (cell_start)
         a.b.cells[key].x = s;
+    if (a.clustered) {
+        // the list of cells holding particles (one entry per cell start),
+        // one atomic per warp
+        const unsigned act = __activemask();
+        const unsigned b = __ballot_sync(act, cell_start);
+        const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+        uint32_t base = 0;
+        if (lane == leader && b)
+            base = atomicAdd(&a.sc->n_chunks, (uint32_t)__popc(b));
+        base = __shfl_sync(act, base, leader);
+        if (cell_start)
+            a.b.work[base + __popc(b & ((1u << lane) - 1u))] = make_uint2(key, s);
+    }
     if (s == N - 1 || a.skeys[s + 1] != key)
         a.b.cells[key].y = s + 1;
 
@@ -376,13 +390,39 @@ k_gather(Consts c, StepArgs a)
     a.b.rho_in[s] = rho_in;
     T.m[s] = m;
     T.p[s] = p;
-    a.b.posq[s] = make_float4(r[0], r[1], D == 3 ? r[2] : 0.f, __int_as_float(im));
-    a.b.velq[s] = make_float4(uh[0], uh[1], D == 3 ? uh[2] : 0.f, rho_h);
-    a.b.pmq[s] = make_float2(p, m);
+    if (a.clustered) {
+        // neighbour records of the clustered sweep: fluid (volume m/rho,
+        // velocity, pressure), boundary element (-area, normal, u.normal),
+        // anything else (0: no neighbour sums)
+        float w0 = 0.f;
+        float4 r1 = make_float4(uh[0], uh[1], D == 3 ? uh[2] : 0.f, p);
+        if (im == 1) {
+            w0 = m / rho_h;
+        } else if (im == -3) {
+            w0 = -m;
+            float un = uh[0] * nrm[0] + uh[1] * nrm[1];
+            if (D == 3)
+                un = un + uh[2] * nrm[2];
+            r1 = make_float4(nrm[0], nrm[1], D == 3 ? nrm[2] : 0.f, un);
+        }
+        a.b.rec0[s] = make_float4(r[0], r[1], D == 3 ? r[2] : 0.f, w0);
+        a.b.rec1[s] = r1;
+    } else {
+        a.b.posq[s] = make_float4(r[0], r[1], D == 3 ? r[2] : 0.f, __int_as_float(im));
+        a.b.velq[s] = make_float4(uh[0], uh[1], D == 3 ? uh[2] : 0.f, rho_h);
+        a.b.pmq[s] = make_float2(p, m);
+    }
     if (im == -3) {
         // the cell's boundary elements lie within [x, y) of its particles
         atomicMin(&a.b.wall_range[key].x, s);
         atomicMax(&a.b.wall_range[key].y, s + 1);
+    }
+    if (c.sample_on && im == 0) {
+        // rate sample: the cells around a probe are always swept
+        const uint32_t nx = a.cs[kc].n_cells[0];
+        const uint32_t nxy = nx * a.cs[kc].n_cells[1];
+        for (int k = 0; k < ((D == 3) ? 27 : 9); k++)
+            a.b.cell_mark[neighbour_cell<D>(key, k, nx, nxy)] = 1;
     }
 }
 
@@ -701,7 +741,8 @@ sweep_particle(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
                          "selp.u32 %0, 1, 0, p;\n}\n"
                          : "=r"(done) : "r"(mb), "r"(par) : "memory");
         phases ^= 1u << b;
-        return __all_sync(0xffffffffu, done != 0);
+        // test switch: a wait that completed counts as timed out
+        return __all_sync(0xffffffffu, done != 0) && !c.debug_fake_timeout;
     };
 
     int k = -1;

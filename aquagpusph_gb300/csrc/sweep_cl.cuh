@@ -1,0 +1,814 @@
+// The clustered neighbour sweep of the fast build (3-D, BIe walls, midpoint
+// scheme): the same sums, rates and integrator as k_sweep
+// (cfd/Interactions.cl:60-145, basic/Shepard.cl:76-125, cfd/Sensors.cl,
+// basic/deltaSPH.cl:191-242,330-350, BIe/{Interactions,Rates,ElasticBounce,
+// PST}.cl, cfd/Rates.cl, midpoint.cl corrector, cfd/TimeStep.cl), with the
+// pair work laid out so that most lanes do useful arithmetic.
+//
+// Work unit: a cell.  A block of NW warps takes the next cell from a work
+// counter and stages the packed records (rec0, rec1: 32 B per particle) of
+// its 3^3-cell neighbourhood into shared memory with bulk copies (the TMA
+// engine, `cp.async.bulk`, completion on an mbarrier).  The neighbourhood is
+// nine contiguous runs of sorted particles (one per (dy, dz) row: the cell
+// keys run x-fastest).
+//
+// Clusters: k_clusters groups each cell's particles by octant into
+// clusters of at most 8 (small octant groups merge).  A warp takes one
+// cluster at a time as 8 particles x 4 neighbour slots: lane l holds
+// particle l / 4 and takes every fourth neighbour of the cluster's list.
+// The list holds the staged candidates within the support of the
+// cluster's bounding box (a lane-parallel filter over the staged records,
+// compacted with ballots), so about 60% of the evaluated pairs lie in the
+// support on a lattice, against about a third of the lanes in k_sweep.
+// Pairs outside the support add exact zeros (the kernel factor is cut to
+// zero at q >= SUPPORT), so the filter only has to be conservative.  The
+// four partial sums of a particle are added by two butterfly shuffles.
+//
+// Summation order differs from the reference's (neighbours in staging
+// order, four interleaved partial sums): this sweep is the fast build's,
+// checked within the per-step rate tolerance 1e-5.  It is deterministic:
+// clusters, lists and staging depend on the sorted state only, not on the
+// launch shape.
+//
+// Boundary elements reach fluid particles through a second list (the BIe
+// wall sums), which also serves the elastic bounce and PST of the
+// epilogue.  Where that list overflowed or the neighbourhood needed more
+// than one staging pass, the epilogue walks the boundary elements of the
+// 27 cells from global memory instead (the per-cell index ranges of k_gather).
+//
+// Probes (imove 0) form clusters of their own; each lane of a probe cluster
+// sums its probe's neighbours in a plain loop over the staged records.
+//
+// With a rate sample (aqua_set_rate_sample) only the cells whose key hashes
+// below the sample's threshold, and the cells around a probe, are swept;
+// the other particles keep what k_gather wrote.
+//
+// This header is included by step_fast.cu only, inside namespace aqua::fast.
+
+namespace {
+
+constexpr int kClListCap = 128;      // fluid survivors per warp (ring of quads)
+constexpr int kClWallCap = 256;      // boundary-element survivors per warp
+constexpr int kClMaxPieces = 32;     // staged runs per pass
+constexpr uint32_t kClWaitLimit = 1u << 22;
+
+// Shared memory of one block: staged records (CAP + 1: the last is a zero
+// record that pads the lists to whole quads), per-warp lists, staged runs
+template<int NW, int CAP>
+struct ClSmem
+{
+    float4 r0[CAP + 1];
+    float4 r1[CAP + 1];
+    uint16_t list[NW][kClListCap + 4];   // + room for the padding quad
+    uint16_t wall[NW][kClWallCap + 4];
+    uint4 piece[kClMaxPieces];   // (slot, sorted first, count, -)
+    uint2 row[9];                // (sorted first, count) of each row
+    uint32_t npieces;
+    uint32_t nstaged;
+    uint32_t total;              // candidates of the neighbourhood
+    uint32_t work;
+    uint64_t mbar;
+};
+
+// Clusters of every cell in the work list: one warp per cell.  The cell's
+// particles are ordered by group (octants 0-7 of the cell, then probes) into
+// cperm[first .. end) and cut into clusters: a group joins the open cluster
+// when it fits whole, else it starts new ones of 8 (probes always start a
+// new cluster).  Ranks within a group follow the sorted order, so the
+// clusters are a function of the sorted state.
+__global__ void __launch_bounds__(256)
+k_clusters(Consts c, StepArgs a)
+{
+    __shared__ uint32_t s_cnt[8][16];
+    __shared__ uint32_t s_pos[8][16];
+    if (a.sc->err)
+        return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t n_work = a.sc->n_chunks;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t w = blockIdx.x * 8u + warp; w < n_work; w += gridDim.x * 8u) {
+        const uint2 wk = a.b.work[w];
+        const uint32_t first = wk.y;
+        const uint32_t end = a.b.cells[wk.x].y;
+        const uint32_t n = end - first;
+        const CaseScalars& cs = a.cs[a.dst.cid[first]];
+        const float sc2 = 2.f * c.idist;
+        auto group = [&](uint32_t s) -> uint32_t {
+            if (a.dst.imove[s] == 0)
+                return 8u;
+            const float4 p = a.b.rec0[s];
+            const uint32_t ox = (uint32_t)((p.x - cs.r_min[0]) * sc2) & 1u;
+            const uint32_t oy = (uint32_t)((p.y - cs.r_min[1]) * sc2) & 1u;
+            const uint32_t oz = (uint32_t)((p.z - cs.r_min[2]) * sc2) & 1u;
+            return ox | (oy << 1) | (oz << 2);
+        };
+        if (lane < 16)
+            s_cnt[warp][lane] = 0;
+        __syncwarp();
+        for (uint32_t b = 0; b < n; b += 32) {
+            const bool v = b + lane < n;
+            const uint32_t g = v ? group(first + b + lane) : 16u;
+            const unsigned m = __match_any_sync(0xffffffffu, g);
+            if (v && lane == __ffs(m) - 1)
+                s_cnt[warp][g] += (uint32_t)__popc(m);
+            __syncwarp();
+        }
+        if (lane == 0) {
+            // the walk over the groups: counts the clusters, then writes them
+            auto walk = [&](bool write, uint32_t k) -> uint32_t {
+                uint32_t pos = 0, coff = 0, ccnt = 0;
+                bool open = false;
+                for (uint32_t g = 0; g < 9; g++) {
+                    const uint32_t cg = s_cnt[warp][g];
+                    if (write)
+                        s_pos[warp][g] = pos;
+                    if (cg == 0)
+                        continue;
+                    if (open && (g == 8 || ccnt + cg > 8)) {
+                        if (write)
+                            a.b.clu[k] = make_uint2(first + coff, ccnt);
+                        k++;
+                        open = false;
+                    }
+                    if (open) {
+                        ccnt += cg;
+                    } else {
+                        uint32_t left = cg, p = pos;
+                        while (left > 8) {
+                            if (write)
+                                a.b.clu[k] = make_uint2(first + p, 8u);
+                            k++;
+                            p += 8;
+                            left -= 8;
+                        }
+                        coff = p;
+                        ccnt = left;
+                        open = true;
+                    }
+                    pos += cg;
+                }
+                if (open) {
+                    if (write)
+                        a.b.clu[k] = make_uint2(first + coff, ccnt);
+                    k++;
+                }
+                return k;
+            };
+            const uint32_t n_cl = walk(false, 0);
+            const uint32_t base = atomicAdd(&a.sc->n_clusters, n_cl);
+            walk(true, base);
+            a.b.wcl[w] = make_uint4(first, end, base, n_cl);
+        }
+        __syncwarp();
+        if (lane < 16)
+            s_cnt[warp][lane] = 0;  // running ranks
+        __syncwarp();
+        for (uint32_t b = 0; b < n; b += 32) {
+            const bool v = b + lane < n;
+            const uint32_t s = first + b + lane;
+            const uint32_t g = v ? group(s) : 16u;
+            const unsigned m = __match_any_sync(0xffffffffu, g);
+            if (v)
+                a.b.cperm[first + s_pos[warp][g] + s_cnt[warp][g] +
+                          (uint32_t)__popc(m & lt)] = s;
+            __syncwarp();
+            if (v && lane == __ffs(m) - 1)
+                s_cnt[warp][g] += (uint32_t)__popc(m);
+            __syncwarp();
+        }
+    }
+}
+
+
+// Everything after the sums for sorted particle i of a cluster (the same
+// steps and expressions as the epilogue of k_sweep): Shepard, the BIe and
+// cfd rates, delta-SPH, elastic bounce, midpoint relax and corrector, PST,
+// the variable time step; returns dt_var (+inf for a lane without a
+// particle).  The four lanes of a particle compute alike; `store` selects
+// the one that writes.  The boundary elements of the elastic bounce and the
+// PST come from the cluster's staged wall list (entries wl[0 .. wfill) of
+// the staged records) or, when `walls_global`, from the per-cell index
+// ranges of the 27 cells around `key` in global memory.
+__device__ __forceinline__ float
+sweep_cl_finish(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
+                int im, bool want, bool fluid, bool sensor, bool store,
+                float dt, const float4 r0i, const float4 r1i, float shep,
+                float gp0, float gp1, float gp2, float lu0, float lu1,
+                float lu2, float du, float lp, float gw0, float gw1, float gw2,
+                float dbi, bool walls_global, const uint16_t* wl,
+                uint32_t wfill, const float4* sr0, const float4* sr1,
+                uint32_t key, const CaseScalars& cas)
+{
+    if (!valid)
+        return INFINITY;
+    const VarSet& T = a.dst;
+    const float hdt = 0.5f * dt;
+    const float rho_i = T.rho[i];
+    const float p_i = r1i.w;
+    if (store && a.b.shepard)
+        a.b.shepard[i] = want ? shep : 0.f;
+    const float4 u4 = reinterpret_cast<const float4*>(T.u)[i];
+    const float ui_full[4] = { u4.x, u4.y, u4.z, u4.w };
+    float gpf[4] = { 0.f, 0.f, 0.f, 0.f }, luf[4] = { 0.f, 0.f, 0.f, 0.f };
+    float gwf[4] = { 0.f, 0.f, 0.f, 0.f };
+    float div_u = 0.f;
+    if (fluid) {
+        // the factors of particle i left out of the pair sums
+        const float ir = 1.f / rho_i;
+        const float ir2 = 2.f * ir;
+        gpf[0] = gp0 * ir;
+        gpf[1] = gp1 * ir;
+        gpf[2] = gp2 * ir;
+        luf[0] = lu0 * ir2;
+        luf[1] = lu1 * ir2;
+        luf[2] = lu2 * ir2;
+        gwf[0] = gw0;
+        gwf[1] = gw1;
+        gwf[2] = gw2;
+        // BIe Rates.cl
+        const float s2 = 2.f * p_i / rho_i;
+        for (int k = 0; k < 4; k++)
+            gpf[k] = gpf[k] + s2 * gwf[k];
+        div_u = du * rho_i - 2.f * rho_i * (dot_full<3>(ui_full, gwf) + dbi);
+    }
+    if (store && a.extras) {
+        Vec<3>::store(a.b.grad_p, i, gpf);
+        Vec<3>::store(a.b.lap_u, i, luf);
+        Vec<3>::store(a.b.grad_w_bi, i, gwf);
+        a.b.div_u[i] = div_u;
+        a.b.lap_p[i] = fluid ? lp : 0.f;
+        a.b.div_u_bi[i] = fluid ? dbi : 0.f;
+    }
+    if (sensor) {
+        // cfd/SensorsRenormalization.cl
+        float shp = shep;
+        if (shp < 1.0e-6f)
+            shp = 1.f;
+        float uo[4] = { gp0, gp1, gp2, ui_full[3] };
+        for (int k = 0; k < 4; k++)
+            uo[k] = uo[k] / shp;
+        if (store) {
+            Vec<3>::store(T.u, i, uo);
+            T.rho[i] = du / shp;
+            T.p[i] = lp / shp;
+        }
+    }
+    if (im <= 0)
+        return c.dt_fixed;
+
+    // boundary elements for the elastic bounce and the PST: f(position,
+    // normal, area); returns early when f returns true
+    const uint32_t nx = cas.n_cells[0];
+    const uint32_t nxy = cas.n_cells[0] * cas.n_cells[1];
+    auto for_walls = [&](auto&& f) {
+        if (!walls_global) {
+            for (uint32_t k = 0; k < wfill; k++) {
+                const uint32_t j = wl[k];
+                const float4 pj = sr0[j];
+                const float4 nj = sr1[j];
+                f(pj, nj, -pj.w);
+            }
+            return;
+        }
+        for (int k = 0; k < 27; k++) {
+            const uint32_t cn = neighbour_cell<3>(key, k, nx, nxy);
+            const uint2 se = a.b.wall_range[cn];  // empty: x > y
+            for (uint32_t j = se.x; j < se.y; j++) {
+                const float4 pj = a.b.rec0[j];
+                if (!(pj.w < 0.f))
+                    continue;
+                const float4 nj = a.b.rec1[j];
+                f(pj, nj, -pj.w);
+            }
+        }
+    };
+
+    const uint32_t set_raw = T.iset[i];
+    const uint32_t set = set_raw < c.n_sets ? set_raw : 0u;
+    float acc[4];
+    float drhodt;
+    float ain[4], uin[4];
+    Vec<3>::load(a.b.dudt_in, i, ain);
+    Vec<3>::load(a.b.u_in, i, uin);
+    const float drhodt_in = a.b.drhodt_in[i];
+    const float ri[3] = { r0i.x, r0i.y, r0i.z };
+    if (fluid) {
+        // cfd Rates.cl + deltaSPH
+        const float visc = c.visc_dyn[set];
+        for (int k = 0; k < 4; k++)
+            acc[k] = -gpf[k] + visc * luf[k] + c.g[k];
+        drhodt = -div_u;
+        const float delta_f = c.delta[set] * dt * rho_i / c.refd[set];
+        drhodt = drhodt + delta_f * lp;
+        // BIe ElasticBounce.cl
+        if (dt != 0.f) {
+            float vh[3];
+            for (int k = 0; k < 3; k++)
+                vh[k] = uin[k] + hdt * acc[k];
+            for_walls([&](const float4 pj, const float4 nj4, float mj) {
+                const float nj[3] = { nj4.x, nj4.y, nj4.z };
+                float d[3], t[3];
+                d[0] = pj.x - ri[0];
+                d[1] = pj.y - ri[1];
+                d[2] = pj.z - ri[2];
+                const float rn = dot_d<3>(d, nj);
+                if (rn < 0.f)
+                    return;
+                const float dr = sqrtf(mj);
+                const float R = c.dr_factor * dr;
+                for (int kk = 0; kk < 3; kk++)
+                    t[kk] = d[kk] - rn * nj[kk];
+                if (dot_d<3>(t, t) >= R * R)
+                    return;
+                const float drn = dt * dot_d<3>(vh, nj);
+                if (drn < 0.f)
+                    return;
+                if (rn - drn <= c.min_bound_dist * dr) {
+                    float v[3], vr[3];
+                    for (int kk = 0; kk < 3; kk++)
+                        v[kk] = uin[kk] + dt * acc[kk];
+                    const float vn2 = 2.f * dot_d<3>(v, nj);
+                    for (int kk = 0; kk < 3; kk++)
+                        vr[kk] = v[kk] - vn2 * nj[kk];
+                    for (int kk = 0; kk < 3; kk++) {
+                        acc[kk] = (vr[kk] - uin[kk]) / dt;
+                        vh[kk] = uin[kk] + hdt * acc[kk];
+                    }
+                }
+            });
+        }
+    } else {
+        Vec<3>::load(T.dudt, i, acc);
+        drhodt = T.drhodt[i];
+    }
+    float rin[4];
+    Vec<3>::load(a.b.r_in, i, rin);
+    // midpoint relax + corrector
+    const float rl = c.relax_midpoint;
+    for (int k = 0; k < 4; k++)
+        acc[k] = rl * ain[k] + (1.f - rl) * acc[k];
+    drhodt = rl * drhodt_in + (1.f - rl) * drhodt;
+    float rn_[4], un[4];
+    const float hdt2 = 0.5f * dt * dt;
+    for (int k = 0; k < 4; k++) {
+        rn_[k] = rin[k] + dt * uin[k] + hdt2 * acc[k];
+        un[k] = uin[k] + dt * acc[k];
+    }
+    const float rho_n = a.b.rho_in[i] + dt * drhodt;
+    // BIe PST.cl
+    if (fluid) {
+        const float Ri = 0.5f * powf(T.m[i] / rho_n, 1.f / c.DIMS);
+        for_walls([&](const float4 pj, const float4 nj4, float mj) {
+            const float nj[3] = { nj4.x, nj4.y, nj4.z };
+            float d[3], t[3];
+            d[0] = pj.x - rn_[0];
+            d[1] = pj.y - rn_[1];
+            d[2] = pj.z - rn_[2];
+            const float rn = dot_d<3>(d, nj);
+            if (fabsf(rn) > Ri)
+                return;
+            const float dr = sqrtf(mj);
+            const float Rj = c.dr_factor * dr;
+            for (int kk = 0; kk < 3; kk++)
+                t[kk] = d[kk] - rn * nj[kk];
+            if (dot_d<3>(t, t) >= Rj * Rj)
+                return;
+            const float sh = rn - Ri;
+            for (int kk = 0; kk < 3; kk++)
+                rn_[kk] = rn_[kk] + sh * nj[kk];
+        });
+    }
+    if (store) {
+        Vec<3>::store(T.dudt, i, acc);
+        T.drhodt[i] = drhodt;
+        Vec<3>::store(T.r, i, rn_);
+        Vec<3>::store(T.u, i, un);
+        T.rho[i] = rho_n;
+    }
+    // TimeStep.cl
+    const float dr_max = c.dt_Ma * c.h;
+    const float dt_u = c.courant * dr_max / sqrtf(dot_full<3>(un, un));
+    return cl_max(cl_min(c.dt_fixed, dt_u), c.dt_min);
+}
+
+__device__ __forceinline__ bool
+cl_wait(uint64_t* mbar, uint32_t parity)
+{
+    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar);
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kClWaitLimit && !done; it++)
+        asm volatile("{\n.reg .pred p;\n"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     "selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(mb), "r"(parity) : "memory");
+    return done != 0;
+}
+
+// The persistent clustered sweep.  NW warps per block, CAP staged records
+// per pass.
+template<int NW, int CAP, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB)
+k_sweep_cl(Consts c, StepArgs a)
+{
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    ClSmem<NW, CAP>& S = *reinterpret_cast<ClSmem<NW, CAP>*>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int q = lane & 3;          // neighbour slot
+    const int mq = lane >> 2;        // particle of the cluster
+    const uint32_t lt = (1u << lane) - 1u;
+    const VarSet& T = a.dst;
+    if (tid == 0) {
+        const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&S.mbar);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(mb));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        S.r0[CAP] = make_float4(0.f, 0.f, 0.f, 0.f);
+        S.r1[CAP] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    uint32_t parity = 0;
+    float run_min = INFINITY;
+    uint32_t run_case = 0xffffffffu;
+    auto flush = [&]() {
+        if (lane == 0 && run_case != 0xffffffffu) {
+            if (run_min < INFINITY && run_min >= 0.f)
+                atomicMin(&a.cs[run_case].dt_next, __float_as_uint(run_min));
+            else if (!(run_min >= 0.f))
+                atomicOr(&a.sc->err, kErrDt);
+        }
+    };
+    const float R2 = c.q2_reject * 1.001f;
+
+    // Stages pass p of the current neighbourhood (the rows' runs as one
+    // sequence, CAP records per pass) and waits for it.  Returns false on a
+    // time-out (recorded in the error word); every thread returns the same.
+    auto stage = [&](uint32_t p) -> bool {
+        if (tid == 0) {
+            const uint32_t lo = p * (uint32_t)CAP;
+            const uint32_t hi = min(S.total, lo + (uint32_t)CAP);
+            uint32_t np = 0, off = 0;
+            for (int r = 0; r < 9; r++) {
+                const uint2 rw = S.row[r];
+                const uint32_t a0 = max(off, lo), a1 = min(off + rw.y, hi);
+                if (a1 > a0 && np < kClMaxPieces) {
+                    S.piece[np++] = make_uint4(a0 - lo, rw.x + (a0 - off), a1 - a0, 0u);
+                }
+                off += rw.y;
+            }
+            S.npieces = np;
+            S.nstaged = hi - lo;
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&S.mbar);
+            // the generic reads of the buffers before the async writes
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n"
+                         :: "r"(mb), "r"((hi - lo) * 32u) : "memory");
+            for (uint32_t k = 0; k < np; k++) {
+                const uint4 pc = S.piece[k];
+                const uint32_t bytes = pc.z * 16u;
+                const uint32_t d0 = (uint32_t)__cvta_generic_to_shared(&S.r0[pc.x]);
+                const uint32_t d1 = (uint32_t)__cvta_generic_to_shared(&S.r1[pc.x]);
+                const uint64_t g0 = (uint64_t)__cvta_generic_to_global(a.b.rec0 + pc.y);
+                const uint64_t g1 = (uint64_t)__cvta_generic_to_global(a.b.rec1 + pc.y);
+                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                             "[%0], [%1], %2, [%3];\n"
+                             :: "r"(d0), "l"(g0), "r"(bytes), "r"(mb) : "memory");
+                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                             "[%0], [%1], %2, [%3];\n"
+                             :: "r"(d1), "l"(g1), "r"(bytes), "r"(mb) : "memory");
+            }
+        }
+        bool ok = cl_wait(&S.mbar, parity);
+        if (!ok)
+            ok = cl_wait(&S.mbar, parity);  // the copies in flight, again bounded
+        else if (c.debug_fake_timeout)
+            ok = false;  // test switch: the copies have completed
+        parity ^= 1u;
+        __syncthreads();  // S.piece / S.nstaged visible; the vote below
+        const bool bad = __syncthreads_or(!ok);
+        if (bad && tid == 0)
+            atomicOr(&a.sc->err, kErrTimeout);
+        return !bad;
+    };
+
+    // sorted index of staged slot k (probe path only)
+    auto sorted_of = [&](uint32_t k) -> uint32_t {
+        for (uint32_t i = 0; i < S.npieces; i++) {
+            const uint4 pc = S.piece[i];
+            if (k >= pc.x && k < pc.x + pc.z)
+                return pc.y + (k - pc.x);
+        }
+        return 0u;
+    };
+
+    const uint32_t n_work = a.sc->n_chunks;
+    for (;;) {
+        // one thread decides for the block (another block may set the error
+        // word at any time: every thread must see the same decision)
+        if (tid == 0) {
+            uint32_t w = a.sc->err ? 0xffffffffu : atomicAdd(&a.sc->chunk_next, 1u);
+            // rate sample: skip the cells outside it
+            while (c.sample_on && w < n_work) {
+                const uint32_t k = a.b.work[w].x;
+                if (sample_hash(k, c.sample_seed) < c.sample_thr || a.b.cell_mark[k])
+                    break;
+                w = atomicAdd(&a.sc->chunk_next, 1u);
+            }
+            S.work = w;
+        }
+        __syncthreads();
+        const uint32_t w = S.work;
+        if (w >= n_work)
+            break;
+        const uint4 wc = a.b.wcl[w];
+        const uint32_t key = a.b.work[w].x;
+        const uint32_t n_cl = wc.w;
+        const uint32_t kc = T.cid[wc.x];
+        const CaseScalars& cas = a.cs[kc];
+        const float dt = cas.dt;
+        if (warp == 0 && lane < 9) {
+            // row (dy, dz) = (lane % 3 - 1, lane / 3 - 1): cells x-1 .. x+1
+            const uint32_t nx = cas.n_cells[0];
+            const uint32_t nxy = cas.n_cells[0] * cas.n_cells[1];
+            const uint32_t k0 = key + (uint32_t)(lane % 3 - 1) * nx +
+                                (uint32_t)(lane / 3 - 1) * nxy - 1u;
+            uint32_t lo = 0xffffffffu, hi = 0;
+            for (int d = 0; d < 3; d++) {
+                const uint2 se = a.b.cells[k0 + d];
+                if (se.x < se.y) {
+                    lo = min(lo, se.x);
+                    hi = max(hi, se.y);
+                }
+            }
+            S.row[lane] = hi > lo ? make_uint2(lo, hi - lo) : make_uint2(0u, 0u);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t t = 0;
+            for (int r = 0; r < 9; r++)
+                t += S.row[r].y;
+            S.total = t;
+        }
+        __syncthreads();
+        const uint32_t npass = (S.total + CAP - 1) / CAP;
+        const bool single = npass <= 1;
+        bool failed = !stage(0);
+        // single pass: each warp takes every NW-th cluster; several passes:
+        // waves of NW clusters, each wave re-staging every pass
+        const uint32_t waves = single ? 1u : (n_cl + NW - 1) / NW;
+        for (uint32_t wave = 0; wave < waves && !failed; wave++) {
+            const uint32_t c_begin = single ? (uint32_t)warp : wave * NW + warp;
+            const uint32_t c_step = single ? (uint32_t)NW : 0xffffffffu;
+            for (uint32_t ci = c_begin; ; ci += c_step) {
+                const bool have = ci < n_cl;
+                if (single && !have)
+                    break;
+                // ---- cluster set-up
+                uint2 cl = make_uint2(0u, 0u);
+                if (have)
+                    cl = a.b.clu[wc.z + ci];
+                const bool valid = (uint32_t)mq < cl.y;
+                const uint32_t i = a.b.cperm[cl.x + (valid ? (uint32_t)mq : 0u)];
+                const float4 r0i = a.b.rec0[i];
+                const float4 r1i = a.b.rec1[i];
+                const int im = T.imove[i];
+                const bool want = valid && im >= -3 && im <= 1;
+                const bool fluid = valid && im == 1;
+                const bool sensor = valid && im == 0;
+                const bool any_fluid = __any_sync(0xffffffffu, fluid);
+                const bool probes = __any_sync(0xffffffffu, sensor);
+                float blo[3], bhi[3];
+                {
+                    const float ri[3] = { r0i.x, r0i.y, r0i.z };
+                    for (int d = 0; d < 3; d++) {
+                        float lo = want ? ri[d] : INFINITY;
+                        float hi = want ? ri[d] : -INFINITY;
+                        for (int o = 16; o > 0; o >>= 1) {
+                            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+                        }
+                        blo[d] = lo;
+                        bhi[d] = hi;
+                    }
+                }
+                const bool any_want = blo[0] <= bhi[0];
+                float shep = 0.f, gp0 = 0.f, gp1 = 0.f, gp2 = 0.f;
+                float lu0 = 0.f, lu1 = 0.f, lu2 = 0.f, du = 0.f, lp = 0.f;
+                float gw0 = 0.f, gw1 = 0.f, gw2 = 0.f, dbi = 0.f;
+                const float pi = r1i.w;
+                uint32_t wfill = 0;
+                bool walls_global = !single;
+                uint16_t* list = S.list[warp];
+                uint16_t* wl = S.wall[warp];
+
+                // one fluid neighbour (staged slot j) of this lane's particle
+                auto fluid_pair = [&](uint32_t j) {
+                    const float4 pj = S.r0[j];
+                    const float4 vj = S.r1[j];
+                    const float d0 = pj.x - r0i.x, d1 = pj.y - r0i.y, d2 = pj.z - r0i.z;
+                    const float rr = d0 * d0 + d1 * d1 + d2 * d2;
+                    const float qq = sqrtf(rr) * c.inv_H;
+                    const float tq = (qq < c.SUPPORT) ? 2.f - qq : 0.f;
+                    const float tq2 = tq * tq;
+                    const float wp = c.w_conw * (1.f + 2.f * qq) * tq2 * tq2;
+                    shep = shep + wp * pj.w;
+                    const float gf = c.f_conf * tq2 * tq * pj.w;
+                    const float dv0 = vj.x - r1i.x, dv1 = vj.y - r1i.y, dv2 = vj.z - r1i.z;
+                    const float udr = dv0 * d0 + dv1 * d1 + dv2 * d2;
+                    const float t = (pi + vj.w) * gf;
+                    gp0 = gp0 + t * d0;
+                    gp1 = gp1 + t * d1;
+                    gp2 = gp2 + t * d2;
+                    lu0 = lu0 + gf * dv0;
+                    lu1 = lu1 + gf * dv1;
+                    lu2 = lu2 + gf * dv2;
+                    du = du + udr * gf;
+                    lp = lp + (vj.w - pi) * gf;
+                };
+                // one boundary element (staged slot j): BIe wall sums
+                auto wall_pair = [&](uint32_t j) {
+                    const float4 pj = S.r0[j];
+                    const float4 nj = S.r1[j];
+                    const float d0 = pj.x - r0i.x, d1 = pj.y - r0i.y, d2 = pj.z - r0i.z;
+                    const float rr = d0 * d0 + d1 * d1 + d2 * d2;
+                    const float qq = sqrtf(rr) * c.inv_H;
+                    const float tq = (qq < c.SUPPORT) ? 2.f - qq : 0.f;
+                    const float tq2 = tq * tq;
+                    const float wa = c.w_conw * (1.f + 2.f * qq) * tq2 * tq2 * (-pj.w);
+                    gw0 = gw0 + nj.x * wa;
+                    gw1 = gw1 + nj.y * wa;
+                    gw2 = gw2 + nj.z * wa;
+                    dbi = dbi - nj.w * wa;
+                };
+                // sums the first nq quads of a list (lane takes slot q)
+                auto drain = [&](const uint16_t* lst, uint32_t nq, bool walls) {
+#pragma unroll 2
+                    for (uint32_t t = 0; t < nq; t++) {
+                        const uint32_t j = lst[4 * t + q];
+                        if (walls)
+                            wall_pair(j);
+                        else
+                            fluid_pair(j);
+                    }
+                };
+
+                for (uint32_t p = 0; p < npass && !failed; p++) {
+                    if (p > 0 || wave > 0) {  // pass 0 of wave 0 is staged
+                        __syncthreads();
+                        failed = !stage(p);
+                        if (failed)
+                            break;
+                    }
+                    if (!have || !any_want)
+                        continue;
+                    const uint32_t nst = S.nstaged;
+                    if (probes) {
+                        // probe cluster: lane m < 8 sums probe m over every
+                        // staged record (cfd/Sensors.cl: fluid neighbours)
+                        const uint32_t ip = a.b.cperm[cl.x + min((uint32_t)lane, cl.y - 1u)];
+                        const float4 rp = a.b.rec0[ip];
+                        float sh = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f, sr = 0.f, sp = 0.f;
+                        if ((uint32_t)lane < cl.y && T.imove[ip] == 0) {
+                            for (uint32_t j = 0; j < nst; j++) {
+                                const float4 pj = S.r0[j];
+                                if (!(pj.w > 0.f))
+                                    continue;
+                                const float d0 = pj.x - rp.x, d1 = pj.y - rp.y, d2 = pj.z - rp.z;
+                                const float qq = sqrtf(d0 * d0 + d1 * d1 + d2 * d2) * c.inv_H;
+                                if (qq >= c.SUPPORT)
+                                    continue;
+                                const float4 vj = S.r1[j];
+                                const float tq = 2.f - qq;
+                                const float tq2 = tq * tq;
+                                const float wp = c.w_conw * (1.f + 2.f * qq) * tq2 * tq2;
+                                const float wj = wp * pj.w;
+                                sh = sh + wj;
+                                s0 = s0 + vj.x * wj;
+                                s1 = s1 + vj.y * wj;
+                                s2 = s2 + vj.z * wj;
+                                sr = sr + wp * T.m[sorted_of(j)];
+                                sp = sp + vj.w * wj;
+                            }
+                        }
+                        // into the quad layout: slot 0 of particle mq
+                        const float v[6] = { sh, s0, s1, s2, sr, sp };
+                        float o[6];
+                        for (int k = 0; k < 6; k++) {
+                            o[k] = __shfl_sync(0xffffffffu, v[k], mq);
+                            if (q != 0)
+                                o[k] = 0.f;
+                        }
+                        shep += o[0];
+                        gp0 += o[1];
+                        gp1 += o[2];
+                        gp2 += o[3];
+                        du += o[4];
+                        lp += o[5];
+                        continue;
+                    }
+                    uint32_t fill = 0;
+                    uint32_t wdone = wfill;  // wall entries already summed
+                    for (uint32_t base = 0; base < nst; base += 32) {
+                        const uint32_t s = base + lane;
+                        bool f = false, wsv = false;
+                        if (s < nst) {
+                            const float4 pc = S.r0[s];
+                            const float bx = fmaxf(fmaxf(blo[0] - pc.x, pc.x - bhi[0]), 0.f);
+                            const float by = fmaxf(fmaxf(blo[1] - pc.y, pc.y - bhi[1]), 0.f);
+                            const float bz = fmaxf(fmaxf(blo[2] - pc.z, pc.z - bhi[2]), 0.f);
+                            const bool near = bx * bx + by * by + bz * bz < R2;
+                            f = near && pc.w > 0.f;
+                            wsv = near && pc.w < 0.f && any_fluid;
+                        }
+                        const unsigned bf = __ballot_sync(0xffffffffu, f);
+                        const unsigned bw = __ballot_sync(0xffffffffu, wsv);
+                        if (f)
+                            list[fill + __popc(bf & lt)] = (uint16_t)s;
+                        fill += (uint32_t)__popc(bf);
+                        if (bw) {
+                            if (wfill + (uint32_t)__popc(bw) > (uint32_t)kClWallCap) {
+                                // the wall list is full: sum it, and let the
+                                // epilogue walk the walls from global memory
+                                __syncwarp();
+                                const uint32_t n = wfill - wdone;
+                                if (lane < (int)((4 - (n & 3)) & 3))
+                                    wl[wfill + lane] = (uint16_t)CAP;
+                                __syncwarp();
+                                drain(wl + wdone, (n + 3) / 4, true);
+                                __syncwarp();
+                                wfill = 0;
+                                wdone = 0;
+                                walls_global = true;
+                            }
+                            if (wsv)
+                                wl[wfill + __popc(bw & lt)] = (uint16_t)s;
+                            wfill += (uint32_t)__popc(bw);
+                        }
+                        if (fill > (uint32_t)(kClListCap - 32)) {
+                            __syncwarp();
+                            const uint32_t nq = fill / 4;
+                            drain(list, nq, false);
+                            __syncwarp();
+                            const uint32_t rem = fill - 4 * nq;
+                            uint16_t mv = 0;
+                            if ((uint32_t)lane < rem)
+                                mv = list[4 * nq + lane];
+                            __syncwarp();
+                            if ((uint32_t)lane < rem)
+                                list[lane] = mv;
+                            fill = rem;
+                        }
+                    }
+                    // the rest of both lists, padded with the zero record
+                    __syncwarp();
+                    if ((uint32_t)lane < ((4u - (fill & 3u)) & 3u))
+                        list[fill + lane] = (uint16_t)CAP;
+                    const uint32_t nw_ = wfill - wdone;
+                    if ((uint32_t)lane < ((4u - (nw_ & 3u)) & 3u))
+                        wl[wfill + lane] = (uint16_t)CAP;
+                    __syncwarp();
+                    drain(list, (fill + 3) / 4, false);
+                    drain(wl + wdone, (nw_ + 3) / 4, true);
+                    __syncwarp();
+                    if (!single)
+                        wfill = 0;  // the staged records are replaced
+                }
+                if (failed)
+                    break;
+                if (have) {
+                    // ---- the four partial sums of each particle
+                    float* acc[13] = { &shep, &gp0, &gp1, &gp2, &lu0, &lu1, &lu2,
+                                       &du, &lp, &gw0, &gw1, &gw2, &dbi };
+#pragma unroll
+                    for (int k = 0; k < 13; k++) {
+                        float v = *acc[k];
+                        v = v + __shfl_xor_sync(0xffffffffu, v, 1);
+                        v = v + __shfl_xor_sync(0xffffffffu, v, 2);
+                        *acc[k] = v;
+                    }
+                    const float v = sweep_cl_finish(
+                        c, a, i, valid, im, want, fluid, sensor, q == 0, dt,
+                        r0i, r1i, shep, gp0, gp1, gp2, lu0, lu1, lu2, du, lp,
+                        gw0, gw1, gw2, dbi, walls_global, wl, wfill, S.r0,
+                        S.r1, key, cas);
+                    float vm = v;
+                    for (int o = 16; o > 0; o >>= 1)
+                        vm = cl_min(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+                    if (kc != run_case) {
+                        flush();
+                        run_case = kc;
+                        run_min = INFINITY;
+                    }
+                    run_min = cl_min(run_min, vm);
+                }
+                if (!single)
+                    break;  // one cluster per warp per wave
+                __syncwarp();
+            }
+        }
+        if (failed)
+            break;
+        __syncthreads();  // the staged records are rewritten for the next cell
+    }
+    flush();
+}
+
+}  // namespace

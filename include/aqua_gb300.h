@@ -310,16 +310,45 @@ aqua_status aqua_radix_sort(aqua_ctx* ctx, uint32_t* keys, uint32_t* perm,
 aqua_status aqua_set_profiling(aqua_ctx* ctx, int on);
 aqua_status aqua_stage_times(aqua_ctx* ctx, float* ms, uint32_t n);
 
+/* Rate sample for judging a proposed state (no counterpart in the
+ * reference): with 0 < fraction < 1, the steps of the fast 3-D build
+ * (clustered sweep) evaluate the neighbour sums, rates and integrator only
+ * for the particles of the cells whose key hashes (sample_hash of the key
+ * and `seed`) below fraction * 2^32, about `fraction` of them, and of every
+ * cell around a probe; the other particles keep the values the gather left
+ * (positions, velocities and densities of the start of the step, the last
+ * rates).  Stepping a state with dt = 0 this way evaluates the plain rates
+ * of that state on the sample.  fraction >= 1 turns it off. */
+aqua_status aqua_set_rate_sample(aqua_ctx* ctx, float fraction, uint32_t seed);
+
+/* Test-only: with `on` = 1, every bounded wait of the library's kernels
+ * (bulk-copy and tensor-core completions on an mbarrier) that completed is
+ * then reported as timed out, so that the time-out path (error word ->
+ * AQUA_ERR_TIMEOUT from aqua_check / the learned entry points, the state
+ * left as it was) runs with no copy or MMA left in flight.  Process-wide;
+ * read when steps are enqueued (a CUDA graph keeps the value it was
+ * captured with).  No counterpart in the reference. */
+aqua_status aqua_debug_fake_timeouts(int on);
+
 /* The stable radix sort of aqua_radix_sort(), for callers that cannot
- * allocate device memory: no context, no cudaMalloc, no allocating library
+ * allocate device memory: a tool inside another runtime's pre-sized step
+ * loop, code running while a stream is captured, a process held to a fixed
+ * device-memory budget.  No context, no cudaMalloc, no allocating library
  * call.  It has no counterpart in the reference.  Its scratch is a
- * fixed-size array of the library (about 12.6 MB, present on every GPU that
- * loads the library until the process exits), so n is limited to
- * AQUA_NOALLOC_SORT_MAX_KEYS; larger n returns AQUA_ERR_CAPACITY.  keys are
- * sorted in place (values below 2^key_bits), perm[s] = original index and
- * inv_perm[orig] = s (either may be NULL).  All calls on a device share the
- * scratch: calls that overlap on the GPU race.  The first call on a device
- * looks the scratch address up; make it before any stream capture. */
+ * fixed-size array of the library, 12.85 MB (3 * 2^20 + 2^16 + 256 32-bit
+ * words), held by every CUDA context that uses it until the context ends,
+ * so n is limited to AQUA_NOALLOC_SORT_MAX_KEYS; larger n returns
+ * AQUA_ERR_CAPACITY.  keys are sorted in place (values below 2^key_bits),
+ * perm[s] = original index and inv_perm[orig] = s (either may be NULL).
+ * All calls in a context share the scratch: calls that overlap on the GPU
+ * race.  The first call in each CUDA context (contexts are told apart by
+ * their unique id, so a driver-API host's own context and a primary context
+ * re-created after cudaDeviceReset each count as new) looks the scratch
+ * address up, and it is also where the array's memory is committed, since
+ * CUDA loads modules lazily: under a fixed budget that first call is the
+ * one that can fail.  Make it before any stream capture; a call that would
+ * need the lookup while `stream` is capturing returns AQUA_ERR_INVALID and
+ * launches nothing. */
 #define AQUA_NOALLOC_SORT_MAX_KEYS (1u << 20)
 aqua_status aqua_radix_sort_noalloc(uint32_t* keys, uint32_t* perm,
                                     uint32_t* inv_perm, uint32_t n,

@@ -222,10 +222,26 @@ def load_ref(dims):
     return Oracle(path) if os.path.exists(path) else None
 
 
+def reference_dir():
+    """The reference source tree (sanguinariojoe/aquagpusph), from the
+    AQUA_REFERENCE_DIR environment variable; None when it is unset or does
+    not name a directory (the tests that read the tree then skip)."""
+    d = os.environ.get("AQUA_REFERENCE_DIR")
+    return d if d and os.path.isdir(d) else None
+
+
 def build_oracle(ref=False):
     import subprocess
-    targets = ["all"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    targets = ["all"]
+    extra = []
+    if ref:
+        d = reference_dir()
+        if d is None:
+            raise RuntimeError("the reference-kernel harness needs the "
+                               "reference tree: set AQUA_REFERENCE_DIR")
+        targets.append("ref")
+        extra = [f"REF={d}"]
+    subprocess.run(["make", "-s", "-C", HERE] + targets + extra, check=True)
 
 
 def free_surface(st: OracleState, sensors, dr: float, dims: int):

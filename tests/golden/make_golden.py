@@ -170,7 +170,10 @@ def make_history_3d():
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else O.reference_dir()
+    if not ref_root:
+        sys.exit("usage: make_golden.py REFERENCE_TREE (or set AQUA_REFERENCE_DIR)")
+    os.environ["AQUA_REFERENCE_DIR"] = ref_root
     O.build_oracle(ref=True)
     if len(sys.argv) > 2 and sys.argv[2] in ("bi", "ie"):
         make_steps_bi(1 if sys.argv[2] == "ie" else 0)

@@ -47,14 +47,31 @@ SHAPES = [(0, 2), (0, 5), (1, 10), (2, 4), (3, 8), (4, 12), (5, 10), (5, 3),
           (12, 8), (13, 18), (14, 9)]
 
 
+# the clustered sweep of the fast 3-D build: its own summation order, the
+# same for every one of its shapes
+SHAPES_CL = [(15, 2), (15, 1), (16, 3), (16, 1), (17, 2), (17, 1), (16, 7)]
+
+
 @pytest.mark.parametrize("fast", [False, True])
 def test_every_launch_shape_gives_identical_state(gpu, fast):
     c = three_d_case()
-    base = run(c, *SHAPES[0], fast=fast)
-    for v, b in SHAPES[1:]:
-        g = run(c, v, b, fast=fast)
-        for name, a in base.state_arrays().items():
-            assert np.array_equal(getattr(g, name), a), (v, b, name)
+    groups = [SHAPES] + ([SHAPES_CL] if fast else [])
+    for shapes in groups:
+        base = run(c, *shapes[0], fast=fast)
+        for v, b in shapes[1:]:
+            g = run(c, v, b, fast=fast)
+            for name, a in base.state_arrays().items():
+                assert np.array_equal(getattr(g, name), a), (v, b, name)
+
+
+def test_clustered_choice_falls_back_where_it_does_not_apply(gpu):
+    """A clustered variant with the exact build runs the direct sweep: the
+    state equals that of the direct sweep's default shape."""
+    c = three_d_case()
+    a = run(c, 16, 3, fast=False)
+    b = run(c, 9, 14, fast=False)
+    for name, x in b.state_arrays().items():
+        assert np.array_equal(getattr(a, name), x), name
 
 
 def test_tuned_shape_matches_oracle(gpu):
@@ -86,6 +103,8 @@ def test_invalid_tuning_is_rejected(gpu):
     sv = Solver(c.params, capacity=c.N)
     with pytest.raises(_lib.AquaError):
         sv.set_tuning(99, 4)
+    with pytest.raises(_lib.AquaError):
+        sv.set_tuning(18, 2)
     with pytest.raises(_lib.AquaError):
         sv.set_tuning(0, 0)
     sv.close()

@@ -10,7 +10,7 @@ import oracle as O
 from aquagpusph_gb300 import particles_io as P
 from aquagpusph_gb300 import reports as R
 
-REF = "/root/reference"
+REF = O.reference_dir()
 
 
 @pytest.fixture(scope="module")
@@ -21,8 +21,8 @@ def lib():
     return _lib.load()
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "tests")),
-                    reason="reference test fixtures not mounted")
+@pytest.mark.skipif(REF is None or not os.path.isdir(os.path.join(REF, "tests")),
+                    reason="reference tree not given (AQUA_REFERENCE_DIR)")
 def test_reads_reference_fixtures_like_the_golden_inputs(lib):
     # the link-list and radix-sort tests' particles.dat (FastASCII), against
     # the arrays the golden fixtures were generated from

@@ -28,7 +28,7 @@ from aquagpusph_gb300 import case as cases
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
-REF_TREE = "/root/reference"
+REF_TREE = O.reference_dir()
 STATE = ("id", "iset", "imove", "r", "normal", "tangent", "binormal", "u",
          "dudt", "rho", "drhodt", "m", "p")
 
@@ -94,8 +94,8 @@ def test_fixture_rates_of_other_particles_keep_the_old_order(dims):
 
 @pytest.fixture(scope="module")
 def ref():
-    if not os.path.isdir(REF_TREE):
-        pytest.skip("reference tree not mounted")
+    if REF_TREE is None:
+        pytest.skip("reference tree not given (AQUA_REFERENCE_DIR)")
     if not (os.path.exists(O.ref_path(2)) and os.path.exists(O.ref_path(3))):
         O.build_oracle(ref=True)
     return {2: O.load_ref(2), 3: O.load_ref(3)}

@@ -79,3 +79,84 @@ def test_noalloc_sort_rejects_oversize(env):
                                      n, 8, None)
     torch.cuda.synchronize()
     assert st == _lib.AQUA_ERR_CAPACITY
+
+
+# A child process without torch: a driver-API host that owns its contexts.
+# It sorts in the device's primary context, in a context of its own, back in
+# the primary one, and in a second context of its own created after the
+# first was destroyed (which may reuse the old handle value).  The scratch
+# array has a different address in every context, so each must look it up
+# again; a result equal to numpy's stable argsort shows that it did.
+_CONTEXT_SCRIPT = r"""
+import ctypes as C
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from aquagpusph_gb300 import _lib
+lib = _lib.load()
+cu = C.CDLL("libcuda.so.1")
+def ok(r, what):
+    assert r == 0, f"{what}: CUresult {r}"
+ok(cu.cuInit(0), "cuInit")
+dev = C.c_int()
+ok(cu.cuDeviceGet(C.byref(dev), 0), "cuDeviceGet")
+primary = C.c_void_p()
+ok(cu.cuDevicePrimaryCtxRetain(C.byref(primary), dev), "retain")
+def new_context():
+    ctx = C.c_void_p()
+    if hasattr(cu, "cuCtxCreate_v2"):
+        ok(cu.cuCtxCreate_v2(C.byref(ctx), 0, dev), "cuCtxCreate_v2")
+    else:
+        ok(cu.cuCtxCreate_v4(C.byref(ctx), None, 0, dev), "cuCtxCreate_v4")
+    ok(cu.cuCtxSetCurrent(ctx), "set current")
+    return ctx
+def sort_here(seed, n, bits):
+    rng = np.random.default_rng(seed)
+    k = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
+    k[: n // 5] = k[n // 2]
+    bufs = []
+    for _ in range(3):
+        p = C.c_uint64()
+        ok(cu.cuMemAlloc_v2(C.byref(p), C.c_size_t(4 * n)), "cuMemAlloc")
+        bufs.append(p)
+    ok(cu.cuMemcpyHtoD_v2(bufs[0], k.ctypes.data_as(C.c_void_p),
+                          C.c_size_t(4 * n)), "HtoD")
+    st = lib.aqua_radix_sort_noalloc(C.c_void_p(bufs[0].value),
+                                     C.c_void_p(bufs[1].value),
+                                     C.c_void_p(bufs[2].value), n, bits, None)
+    assert st == 0, st
+    ok(cu.cuCtxSynchronize(), "sync")
+    out = [np.empty(n, np.uint32) for _ in range(3)]
+    for o, b in zip(out, bufs):
+        ok(cu.cuMemcpyDtoH_v2(o.ctypes.data_as(C.c_void_p), b,
+                              C.c_size_t(4 * n)), "DtoH")
+        ok(cu.cuMemFree_v2(b), "cuMemFree")
+    ref = np.argsort(k, kind="stable").astype(np.uint32)
+    assert np.array_equal(out[1], ref), "perm"
+    assert np.array_equal(out[0], k[ref]), "keys"
+    inv = np.empty(n, np.uint32)
+    inv[ref] = np.arange(n, dtype=np.uint32)
+    assert np.array_equal(out[2], inv), "inverse perm"
+ok(cu.cuCtxSetCurrent(primary), "set primary")
+sort_here(1, 300_001, 20)
+own = new_context()
+sort_here(2, 654_321, 24)
+ok(cu.cuCtxSetCurrent(primary), "set primary")
+sort_here(3, 99_999, 12)
+ok(cu.cuCtxDestroy_v2(own), "destroy")
+own = new_context()
+sort_here(4, 1 << 20, 24)
+ok(cu.cuCtxDestroy_v2(own), "destroy")
+ok(cu.cuDevicePrimaryCtxRelease_v2(dev), "release")
+print("contexts ok")
+"""
+
+
+def test_noalloc_sort_in_each_cuda_context(env):
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _CONTEXT_SCRIPT, root],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "contexts ok" in r.stdout, r.stdout + r.stderr
