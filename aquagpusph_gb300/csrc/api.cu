@@ -168,6 +168,7 @@ build_consts(const aqua_params* p, Consts& c)
     c.inv_H = 1.f / p->H;
     c.w_conw = (p->dims == 3 ? WendlandC<3>::W : WendlandC<2>::W) * p->CONW;
     c.f_conf = (p->dims == 3 ? WendlandC<3>::F : WendlandC<2>::F) * p->CONF;
+    c.f_over_w = c.f_conf / c.w_conw;
     return AQUA_OK;
 }
 
@@ -312,7 +313,8 @@ sweep_clustered(const aqua_ctx* x)
 {
     return x->fast && x->dims == 3 && x->sweep_variant >= kSweepClustered &&
            x->consts.boundary == AQUA_BOUNDARY_BIE &&
-           x->consts.scheme == AQUA_SCHEME_MIDPOINT;
+           x->consts.scheme == AQUA_SCHEME_MIDPOINT &&
+           x->consts.SUPPORT == 2.f;  // the Wendland support
 }
 
 // Launches one step on `s` (the resident state advances from set[cur] to

@@ -54,6 +54,7 @@ struct Consts
     float inv_H;        // 1 / H
     float w_conw;       // W factor of the Wendland kernel * CONW
     float f_conf;       // F factor * CONF
+    float f_over_w;     // f_conf / w_conw (clustered sweep)
     // test-only: a bounded wait that completed is reported as timed out
     // (AQUA_ERR_TIMEOUT), so the error path runs with nothing in flight
     uint32_t debug_fake_timeout;
@@ -171,7 +172,8 @@ struct StepBufs
     float* div_u_bi;
     float* shepard;
     // clustered sweep (fast build, 3-D): per sorted particle two 16-byte
-    // neighbour records, rec0 = (x, y, z, w) with w = m/rho (fluid), -m
+    // neighbour records, rec0 = (x, y, z, w) with w = CONW * W-factor * m/rho
+    // (fluid), -m
     // (boundary element, its area) or 0 (no neighbour sums), rec1 = (u, p)
     // (fluid) or (normal, u.normal) (boundary element); the cells holding
     // particles as (key, first sorted index) in `work`, their cluster

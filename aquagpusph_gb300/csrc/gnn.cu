@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "aqua_learned.h"
+#include "aqua_internal.cuh"  // sample_hash: the cells of a rate sample
 
 namespace {
 
@@ -1237,6 +1238,39 @@ k_sample_max_diff(uint32_t n, const float* __restrict__ a,
         atomicMax(out, __float_as_int(mx));
 }
 
+// The rate-sample judge of a proposal (see aqua_gnn_judge_density)
+__global__ void
+k_judge_density(uint32_t n, const uint32_t* __restrict__ id1,
+                const uint32_t* __restrict__ icell1,
+                const int32_t* __restrict__ imove1,
+                const float* __restrict__ drhodt1,
+                const uint32_t* __restrict__ icell0,
+                const float* __restrict__ drhodt0,
+                const float* __restrict__ rho0, const float* __restrict__ rho1,
+                float half_kdt, float scale, uint32_t below, uint32_t seed,
+                float* __restrict__ rho_judged, int* out)
+{
+    float mx = 0.f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const uint32_t o = id1[i];
+        const bool both = aqua::sample_hash(icell1[i], seed) < below &&
+                          aqua::sample_hash(icell0[o], seed) < below;
+        const float rj = rho0[o] + half_kdt * (drhodt0[o] + drhodt1[i]);
+        rho_judged[o] = rj;
+        if (imove1[i] != 1 || !both)
+            continue;
+        float d = fabsf(rho1[o] - rj) * scale;
+        if (!(d <= 3.0e38f))
+            d = INFINITY;
+        mx = fmaxf(mx, d);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > 0.f)
+        atomicMax(out, __float_as_int(mx));
+}
+
 __global__ void
 k_case_max_diff(uint32_t n_cases, const uint32_t* __restrict__ off,
                 const float* __restrict__ a, const float* __restrict__ b,
@@ -1792,6 +1826,31 @@ aqua_gnn_sample_max_diff(uint32_t n, const float* a, const float* b,
     const uint32_t below = f >= 4294967295.0 ? 0xffffffffu : (uint32_t)f;
     k_sample_max_diff<<<blocks_for(n, 256, 152u * 8u), 256, 0, s>>>(
         n, a, b, imove, seed, below, scale, reinterpret_cast<int*>(out));
+    return last_error();
+}
+
+aqua_status
+aqua_gnn_judge_density(uint32_t n, const uint32_t* id1, const uint32_t* icell1,
+                       const int32_t* imove1, const float* drhodt1,
+                       const uint32_t* icell0, const float* drhodt0,
+                       const float* rho0, const float* rho1, float kdt,
+                       float scale, float fraction, uint32_t seed,
+                       float* rho_judged, float* out, void* stream)
+{
+    if (!id1 || !icell1 || !imove1 || !drhodt1 || !icell0 || !drhodt0 ||
+        !rho0 || !rho1 || !rho_judged || !out ||
+        !(fraction > 0.f && fraction < 1.f))
+        return AQUA_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaMemsetAsync(out, 0, sizeof(float), s) != cudaSuccess)
+        return AQUA_ERR_CUDA;
+    if (n == 0)
+        return AQUA_OK;
+    // the threshold of aqua_set_rate_sample
+    const uint32_t below = (uint32_t)((double)fraction * 4294967296.0);
+    k_judge_density<<<blocks_for(n, 256, 152u * 8u), 256, 0, s>>>(
+        n, id1, icell1, imove1, drhodt1, icell0, drhodt0, rho0, rho1,
+        0.5f * kdt, scale, below, seed, rho_judged, reinterpret_cast<int*>(out));
     return last_error();
 }
 

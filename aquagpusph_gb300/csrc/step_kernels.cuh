@@ -391,13 +391,14 @@ k_gather(Consts c, StepArgs a)
     T.m[s] = m;
     T.p[s] = p;
     if (a.clustered) {
-        // neighbour records of the clustered sweep: fluid (volume m/rho,
-        // velocity, pressure), boundary element (-area, normal, u.normal),
-        // anything else (0: no neighbour sums)
+        // neighbour records of the clustered sweep: fluid (volume m/rho
+        // times the kernel's CONW W-factor, velocity, pressure), boundary
+        // element (-area, normal, u.normal), anything else (0: no neighbour
+        // sums)
         float w0 = 0.f;
         float4 r1 = make_float4(uh[0], uh[1], D == 3 ? uh[2] : 0.f, p);
         if (im == 1) {
-            w0 = m / rho_h;
+            w0 = c.w_conw * (m / rho_h);  // CONW W-factor * volume
         } else if (im == -3) {
             w0 = -m;
             float un = uh[0] * nrm[0] + uh[1] * nrm[1];

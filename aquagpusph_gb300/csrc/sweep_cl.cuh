@@ -48,7 +48,7 @@
 namespace {
 
 constexpr int kClListCap = 128;      // fluid survivors per warp (ring of quads)
-constexpr int kClWallCap = 256;      // boundary-element survivors per warp
+constexpr int kClWallCap = 192;      // boundary-element survivors per warp
 constexpr int kClMaxPieces = 32;     // staged runs per pass
 constexpr uint32_t kClWaitLimit = 1u << 22;
 
@@ -61,6 +61,9 @@ struct ClSmem
     float4 r1[CAP + 1];
     uint16_t list[NW][kClListCap + 4];   // + room for the padding quad
     uint16_t wall[NW][kClWallCap + 4];
+    // the staged boundary elements, by warp-sized chunks of the staging
+    uint16_t wsub[NW][((CAP + NW * 32 - 1) / (NW * 32)) * 32];
+    uint32_t wcnt[NW];
     uint4 piece[kClMaxPieces];   // (slot, sorted first, count, -)
     uint2 row[9];                // (sorted first, count) of each row
     uint32_t npieces;
@@ -213,8 +216,11 @@ sweep_cl_finish(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     float gwf[4] = { 0.f, 0.f, 0.f, 0.f };
     float div_u = 0.f;
     if (fluid) {
-        // the factors of particle i left out of the pair sums
-        const float ir = 1.f / rho_i;
+        // the factors left out of the pair sums: those of particle i, and
+        // CONF F-factor / (CONW W-factor) (the staged volumes carry the
+        // latter)
+        const float kf = c.f_over_w;
+        const float ir = kf / rho_i;
         const float ir2 = 2.f * ir;
         gpf[0] = gp0 * ir;
         gpf[1] = gp1 * ir;
@@ -222,6 +228,8 @@ sweep_cl_finish(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         luf[0] = lu0 * ir2;
         luf[1] = lu1 * ir2;
         luf[2] = lu2 * ir2;
+        du = du * kf;
+        lp = lp * kf;
         gwf[0] = gw0;
         gwf[1] = gw1;
         gwf[2] = gw2;
@@ -484,9 +492,33 @@ k_sweep_cl(Consts c, StepArgs a)
         parity ^= 1u;
         __syncthreads();  // S.piece / S.nstaged visible; the vote below
         const bool bad = __syncthreads_or(!ok);
-        if (bad && tid == 0)
-            atomicOr(&a.sc->err, kErrTimeout);
-        return !bad;
+        if (bad) {
+            if (tid == 0)
+                atomicOr(&a.sc->err, kErrTimeout);
+            return false;
+        }
+        // the boundary elements among the staged records (few): warp w
+        // lists those of its chunk, in staging order
+        {
+            const uint32_t nst = S.nstaged;
+            constexpr uint32_t kChunk = ((CAP + NW * 32 - 1) / (NW * 32)) * 32;
+            const uint32_t chunk = ((nst + NW * 32 - 1) / (NW * 32)) * 32;
+            const uint32_t lo = (uint32_t)warp * chunk;
+            const uint32_t hi = min(nst, lo + chunk);
+            uint32_t cnt = 0;
+            for (uint32_t b = lo; b < hi; b += 32) {
+                const uint32_t k = b + lane;
+                const bool w = k < hi && S.r0[k].w < 0.f;
+                const unsigned bal = __ballot_sync(0xffffffffu, w);
+                if (w && cnt + __popc(bal & lt) < kChunk)
+                    S.wsub[warp][cnt + __popc(bal & lt)] = (uint16_t)k;
+                cnt += (uint32_t)__popc(bal);
+            }
+            if (lane == 0)
+                S.wcnt[warp] = cnt;
+        }
+        __syncthreads();
+        return true;
     };
 
     // sorted index of staged slot k (probe path only)
@@ -590,6 +622,11 @@ k_sweep_cl(Consts c, StepArgs a)
                     }
                 }
                 const bool any_want = blo[0] <= bhi[0];
+                float bc[3], be[3];  // box centre and half-extent
+                for (int d = 0; d < 3; d++) {
+                    bc[d] = 0.5f * (blo[d] + bhi[d]);
+                    be[d] = 0.5f * (bhi[d] - blo[d]);
+                }
                 float shep = 0.f, gp0 = 0.f, gp1 = 0.f, gp2 = 0.f;
                 float lu0 = 0.f, lu1 = 0.f, lu2 = 0.f, du = 0.f, lp = 0.f;
                 float gw0 = 0.f, gw1 = 0.f, gw2 = 0.f, dbi = 0.f;
@@ -606,11 +643,13 @@ k_sweep_cl(Consts c, StepArgs a)
                     const float d0 = pj.x - r0i.x, d1 = pj.y - r0i.y, d2 = pj.z - r0i.z;
                     const float rr = d0 * d0 + d1 * d1 + d2 * d2;
                     const float qq = sqrtf(rr) * c.inv_H;
-                    const float tq = (qq < c.SUPPORT) ? 2.f - qq : 0.f;
+                    // (2 - q)^+: zero at and beyond the support (2)
+                    const float tq = fmaxf(2.f - qq, 0.f);
                     const float tq2 = tq * tq;
-                    const float wp = c.w_conw * (1.f + 2.f * qq) * tq2 * tq2;
-                    shep = shep + wp * pj.w;
-                    const float gf = c.f_conf * tq2 * tq * pj.w;
+                    // pj.w = CONW W-factor * m/rho: W(q) CONW m/rho, and
+                    // F(q) CONF m/rho up to the factor f_over_w
+                    shep = shep + (1.f + 2.f * qq) * tq2 * tq2 * pj.w;
+                    const float gf = tq2 * tq * pj.w;
                     const float dv0 = vj.x - r1i.x, dv1 = vj.y - r1i.y, dv2 = vj.z - r1i.z;
                     const float udr = dv0 * d0 + dv1 * d1 + dv2 * d2;
                     const float t = (pi + vj.w) * gf;
@@ -630,7 +669,7 @@ k_sweep_cl(Consts c, StepArgs a)
                     const float d0 = pj.x - r0i.x, d1 = pj.y - r0i.y, d2 = pj.z - r0i.z;
                     const float rr = d0 * d0 + d1 * d1 + d2 * d2;
                     const float qq = sqrtf(rr) * c.inv_H;
-                    const float tq = (qq < c.SUPPORT) ? 2.f - qq : 0.f;
+                    const float tq = fmaxf(2.f - qq, 0.f);
                     const float tq2 = tq * tq;
                     const float wa = c.w_conw * (1.f + 2.f * qq) * tq2 * tq2 * (-pj.w);
                     gw0 = gw0 + nj.x * wa;
@@ -678,8 +717,9 @@ k_sweep_cl(Consts c, StepArgs a)
                                 const float4 vj = S.r1[j];
                                 const float tq = 2.f - qq;
                                 const float tq2 = tq * tq;
-                                const float wp = c.w_conw * (1.f + 2.f * qq) * tq2 * tq2;
-                                const float wj = wp * pj.w;
+                                const float wq = (1.f + 2.f * qq) * tq2 * tq2;
+                                const float wp = c.w_conw * wq;
+                                const float wj = wq * pj.w;
                                 sh = sh + wj;
                                 s0 = s0 + vj.x * wj;
                                 s1 = s1 + vj.y * wj;
@@ -708,22 +748,51 @@ k_sweep_cl(Consts c, StepArgs a)
                     uint32_t wdone = wfill;  // wall entries already summed
                     for (uint32_t base = 0; base < nst; base += 32) {
                         const uint32_t s = base + lane;
-                        bool f = false, wsv = false;
+                        bool f = false;
                         if (s < nst) {
                             const float4 pc = S.r0[s];
-                            const float bx = fmaxf(fmaxf(blo[0] - pc.x, pc.x - bhi[0]), 0.f);
-                            const float by = fmaxf(fmaxf(blo[1] - pc.y, pc.y - bhi[1]), 0.f);
-                            const float bz = fmaxf(fmaxf(blo[2] - pc.z, pc.z - bhi[2]), 0.f);
-                            const bool near = bx * bx + by * by + bz * bz < R2;
-                            f = near && pc.w > 0.f;
-                            wsv = near && pc.w < 0.f && any_fluid;
+                            const float bx = fmaxf(fabsf(pc.x - bc[0]) - be[0], 0.f);
+                            const float by = fmaxf(fabsf(pc.y - bc[1]) - be[1], 0.f);
+                            const float bz = fmaxf(fabsf(pc.z - bc[2]) - be[2], 0.f);
+                            f = (bx * bx + by * by + bz * bz < R2) && pc.w > 0.f;
                         }
                         const unsigned bf = __ballot_sync(0xffffffffu, f);
-                        const unsigned bw = __ballot_sync(0xffffffffu, wsv);
                         if (f)
                             list[fill + __popc(bf & lt)] = (uint16_t)s;
                         fill += (uint32_t)__popc(bf);
-                        if (bw) {
+                        if (fill > (uint32_t)(kClListCap - 32)) {
+                            __syncwarp();
+                            const uint32_t nq = fill / 4;
+                            drain(list, nq, false);
+                            __syncwarp();
+                            const uint32_t rem = fill - 4 * nq;
+                            uint16_t mv = 0;
+                            if ((uint32_t)lane < rem)
+                                mv = list[4 * nq + lane];
+                            __syncwarp();
+                            if ((uint32_t)lane < rem)
+                                list[lane] = mv;
+                            fill = rem;
+                        }
+                    }
+                    // boundary elements (fluid clusters only): the staged
+                    // wall sub-lists in order
+                    for (int ws = 0; any_fluid && ws < NW; ws++) {
+                        const uint32_t wn = min(S.wcnt[ws], (uint32_t)(sizeof(S.wsub[0]) / 2));
+                        for (uint32_t b = 0; b < wn; b += 32) {
+                            bool wsv = false;
+                            uint32_t s = 0;
+                            if (b + lane < wn) {
+                                s = S.wsub[ws][b + lane];
+                                const float4 pc = S.r0[s];
+                                const float bx = fmaxf(fabsf(pc.x - bc[0]) - be[0], 0.f);
+                                const float by = fmaxf(fabsf(pc.y - bc[1]) - be[1], 0.f);
+                                const float bz = fmaxf(fabsf(pc.z - bc[2]) - be[2], 0.f);
+                                wsv = bx * bx + by * by + bz * bz < R2;
+                            }
+                            const unsigned bw = __ballot_sync(0xffffffffu, wsv);
+                            if (!bw)
+                                continue;
                             if (wfill + (uint32_t)__popc(bw) > (uint32_t)kClWallCap) {
                                 // the wall list is full: sum it, and let the
                                 // epilogue walk the walls from global memory
@@ -741,20 +810,6 @@ k_sweep_cl(Consts c, StepArgs a)
                             if (wsv)
                                 wl[wfill + __popc(bw & lt)] = (uint16_t)s;
                             wfill += (uint32_t)__popc(bw);
-                        }
-                        if (fill > (uint32_t)(kClListCap - 32)) {
-                            __syncwarp();
-                            const uint32_t nq = fill / 4;
-                            drain(list, nq, false);
-                            __syncwarp();
-                            const uint32_t rem = fill - 4 * nq;
-                            uint16_t mv = 0;
-                            if ((uint32_t)lane < rem)
-                                mv = list[4 * nq + lane];
-                            __syncwarp();
-                            if ((uint32_t)lane < rem)
-                                list[lane] = mv;
-                            fill = rem;
                         }
                     }
                     // the rest of both lists, padded with the zero record

@@ -133,6 +133,8 @@ SIGNATURES = {
     "aqua_gnn_sample_max_diff": [_u32, _vp, _vp, _vp, _u32, _f32, _f32, _vp,
                                  _vp],
     "aqua_gnn_case_max_diff": [_u32, _vp, _vp, _vp, _vp, _f32, _vp, _vp],
+    "aqua_gnn_judge_density": [_u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                               _f32, _f32, _f32, _u32, _vp, _vp, _vp],
 }
 
 
@@ -842,6 +844,9 @@ class ProposalRunner:
         self.stats = {"proposals": 0, "judged": 0, "rolled_back": 0,
                       "p_err": [], "rho_err": []}
 
+    def close(self):
+        self.judge.close()
+
     def _motion_arrays(self, scal, T):
         torch = _torch()
         n = len(self.batch.motions)
@@ -990,18 +995,24 @@ class ProposalRunner:
 
 class FieldProposalRunner:
     """Advances one large case by learned k-step proposals, each judged by
-    the plain step over the whole field.
+    the plain method on a 10% sample.
 
     Each ``advance()``: the network proposes the state k plain steps ahead
     (graph radius ``radius``, default 0.9 h: with h = 2 dx, the 26 nearest
-    lattice neighbours); the plain step re-runs the same k
-    steps from the same state in a second solver context; the proposal is
-    compared with it at every probe of the case (Shepard-interpolated
-    pressure, ``aqua_gnn_probes_pressure``) and, for density, on a random
-    subsample of ``rho_sample`` of the fluid particles drawn anew each time.
-    If a probe departs by more than ``tol`` of max(|p_plain|, p_floor), or
-    the subsample's density by more than ``tol`` of refd, the whole field
-    takes the plain state (rollback); otherwise the proposal stands."""
+    lattice neighbours).  The judge evaluates the plain rates (one step of
+    the plain pipeline, cfd/Rates.cl:55-77 with basic/deltaSPH.cl:330-350)
+    at the start state and at the proposed state, each on the same hashed
+    sample of the cells (a fraction ``rho_sample`` of them, drawn anew each
+    proposal, plus every cell around a probe: ``aqua_set_rate_sample``), in
+    a second solver context.  Over the k steps the plain continuity
+    equation gives each sampled particle the density rho0 + k dt (drho/dt0
+    + drho/dt1) / 2 (trapezoidal rule); the proposal fails where a sampled
+    fluid particle's proposed density departs from it by more than ``tol``
+    of refd, or where a probe's pressure (Shepard-interpolated,
+    ``aqua_gnn_probes_pressure``) from the proposed densities departs by
+    more than ``tol`` of max(|p|, p_floor) from the same interpolation of
+    the plain densities.  A failed proposal is rolled back: the resident
+    state, still the start state, is advanced by k plain steps instead."""
 
     def __init__(self, solver, case, model, k=8, radius=None, rho_sample=0.1,
                  tol=0.02, p_floor=None, seed=0, fast=True):
@@ -1032,6 +1043,13 @@ class FieldProposalRunner:
                                    device="cuda")
         self.judge = Solver(p, capacity=case.N)
         self.judge.set_precision(fast)
+        n = case.N
+        self._icell = torch.empty(n, dtype=torch.int32, device="cuda")
+        self._raw = Snapshot(n, self.dims)
+        self._icell0 = torch.empty(n, dtype=torch.int32, device="cuda")
+        self._drho0 = torch.empty(n, dtype=torch.float32, device="cuda")
+        self._rho_j = torch.empty(n, dtype=torch.float32, device="cuda")
+        self._res = torch.empty(1, dtype=torch.float32, device="cuda")
         self.stats = {"proposals": 0, "rolled_back": 0, "p_err": [],
                       "rho_err": [], "n_edges": 0, "phase_s": {}}
 
@@ -1043,38 +1061,38 @@ class FieldProposalRunner:
         ph[name] = ph.get(name, 0.0) + (t1 - t0)
         return t1
 
-    def probe_pressures(self, snap):
-        """Pressure at every probe of a snapshot (device, one per probe)."""
+    def probe_pressures(self, snap, rho=None):
+        """Pressure at every probe of a snapshot (device, one per probe),
+        from the snapshot's densities or from `rho` (by particle id)."""
         torch = _torch()
         out = torch.empty(len(self.probes), dtype=torch.float32, device="cuda")
         _chk("aqua_gnn_probes_pressure", lib().aqua_gnn_probes_pressure(
-            snap.n, self.dims, _p(snap["r"]), _p(snap["rho"]), _p(snap["m"]),
-            _p(snap["imove"]), len(self.probes), _p(self.probes), self.consts,
-            _p(self.scratch), _p(out), _vp(0)))
+            snap.n, self.dims, _p(snap["r"]), _p(snap["rho"] if rho is None else rho),
+            _p(snap["m"]), _p(snap["imove"]), len(self.probes), _p(self.probes),
+            self.consts, _p(self.scratch), _p(out), _vp(0)))
         return out
 
-    def _rho_err(self, a, b, imove):
-        """max |rho_a - rho_b| / refd over a fresh random subsample (a
-        fraction rho_sample) of the fluid particles."""
-        torch = _torch()
-        er = torch.empty(1, dtype=torch.float32, device="cuda")
-        seed = int(self.rng.integers(0, 2 ** 32))
-        _chk("aqua_gnn_sample_max_diff", lib().aqua_gnn_sample_max_diff(
-            self.n, _p(a), _p(b), _p(imove), seed, self.rho_sample,
-            1.0 / self.refd, _p(er), _vp(0)))
-        return float(er.item())
+    def _plain_rates(self, snap, sc):
+        """One plain step of the judge context from `snap` with the rate
+        sample on; leaves its sorted state in self._raw and its cell keys in
+        self._icell."""
+        self.judge.set_state_raw(self.n, snap.ptrs(), False, sc["t"], sc["dt"],
+                                 sc["iter"])
+        self.judge.step(1, graph=False)
+        self.judge.check()
+        self.judge.get_state_raw(self._raw.ptrs(), False)
+        self.judge.get_icell_raw(self._icell.data_ptr())
 
     def advance(self):
         """One proposal of k steps (synchronises)."""
         torch = _torch()
         L = lib()
-        dims, k = self.dims, self.k
+        dims, k, n = self.dims, self.k, self.n
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sc = self.sv.scalars()
         dt = torch.tensor([sc["dt"]], dtype=torch.float32, device="cuda")
         s0 = Snapshot.capture(self.sv, dims)
-        n = s0.n
         t0 = self._phase("snapshot", t0)
         # ---- proposal
         g = Graph(self.sv, dims, s0["r"], s0["imove"], self.cid, n, self.radius)
@@ -1091,28 +1109,37 @@ class FieldProposalRunner:
             _p(s0["drhodt"]), _p(s0["imove"]), _vp(0)))
         del x, out, g
         t0 = self._phase("network", t0)
-        # ---- plain judge over the whole field, from the same state
-        self.judge.set_state_raw(n, s0.ptrs(), False, sc["t"], sc["dt"],
-                                 sc["iter"])
-        self.judge.step(k, graph=True)
-        self.judge.check()
-        t0 = self._phase("judge", t0)
-        plain = Snapshot.capture(self.judge, dims)
+        # ---- judge: plain rates at both ends on one cell sample
+        seed = int(self.rng.integers(0, 2 ** 32))
+        self.judge.set_rate_sample(self.rho_sample, seed)
+        self._plain_rates(s0, sc)
+        raw = self._raw
+        _chk("aqua_gnn_scatter32", L.aqua_gnn_scatter32(
+            n, _p(raw["id"]), _p(self._icell), 1, _p(self._icell0), 1, _vp(0)))
+        _chk("aqua_gnn_scatter32", L.aqua_gnn_scatter32(
+            n, _p(raw["id"]), _p(raw["drhodt"]), 1, _p(self._drho0), 1, _vp(0)))
+        self._plain_rates(s1, sc)
+        _chk("aqua_gnn_judge_density", L.aqua_gnn_judge_density(
+            n, _p(raw["id"]), _p(self._icell), _p(raw["imove"]),
+            _p(raw["drhodt"]), _p(self._icell0), _p(self._drho0),
+            _p(s0["rho"]), _p(s1["rho"]), float(k * sc["dt"]), 1.0 / self.refd,
+            self.rho_sample, seed, _p(self._rho_j), _p(self._res), _vp(0)))
         pp = self.probe_pressures(s1).cpu().numpy()
-        pj = self.probe_pressures(plain).cpu().numpy()
+        pj = self.probe_pressures(s1, self._rho_j).cpu().numpy()
         p_err = np.abs(pp - pj) / np.maximum(np.abs(pj), self.p_floor)
-        rho_err = self._rho_err(s1["rho"], plain["rho"], plain["imove"])
+        rho_err = float(self._res.item())
         bad = bool((p_err > self.tol).any() or rho_err > self.tol)
-        t0 = self._phase("compare", t0)
-        # ---- rollback (the plain field) or the proposal becomes resident
+        t0 = self._phase("judge", t0)
+        # ---- rollback (k plain steps from the start state, which is still
+        # resident) or the proposal becomes resident
         if bad:
-            js = self.judge.scalars()
-            self.sv.set_state_raw(n, plain.ptrs(), False, js["t"], js["dt"],
-                                  js["iter"])
+            self.sv.step(k, graph=True)
+            self.sv.check()
+            t0 = self._phase("rollback", t0)
         else:
             self.sv.set_state_raw(n, s1.ptrs(), False, sc["t"] + k * sc["dt"],
                                   sc["dt"], sc["iter"] + k)
-        self._phase("set_state", t0)
+            t0 = self._phase("set_state", t0)
         st = self.stats
         st["proposals"] += 1
         st["rolled_back"] += int(bad)

@@ -62,6 +62,20 @@ class Solver:
         _lib.check("aqua_set_precision",
                    self.lib.aqua_set_precision(self.ctx, mode))
 
+    def set_rate_sample(self, fraction: float, seed: int = 0):
+        """Steps evaluate the sums and rates only on a hashed sample of the
+        cells (about `fraction` of them) and the cells around the probes
+        (fast 3-D build); fraction >= 1 turns it off."""
+        _lib.check("aqua_set_rate_sample", self.lib.aqua_set_rate_sample(
+            self.ctx, float(fraction), int(seed) & 0xFFFFFFFF))
+
+    def get_icell_raw(self, ptr: int, stream=None):
+        """The sorted cell keys of the last step (device address, N uint32)."""
+        e = _lib.AquaExtra()
+        e.icell = C.cast(C.c_void_p(ptr), _lib._U)
+        _lib.check("aqua_get_extra", self.lib.aqua_get_extra(
+            self.ctx, C.byref(e), 0, C.c_void_p(stream or 0)))
+
     def set_tuning(self, sweep_variant: int, blocks_per_sm: int):
         """Launch shape of the sweep (results do not depend on it)."""
         _lib.check("aqua_set_tuning", self.lib.aqua_set_tuning(

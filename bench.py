@@ -218,8 +218,34 @@ def job_throughput(world: int, n_per_rank: int, steps: int, seconds: float) -> f
 
 # DRAM bytes per particle of the fused sweep from one ncu capture of the
 # 1.89M-particle profiling case (dram__bytes_read.sum + dram__bytes_write.sum
-# over N; profiles/k_sweep_c1m.md), scaled to a launch by N.
-SWEEP_DRAM_BYTES_PER_PARTICLE = {"k_sweep<3>": 170.5}
+# over N; profiles/k_sweep_cl_c1m.md, profiles/k_sweep_c1m.md), scaled to a
+# launch by N.
+SWEEP_DRAM_BYTES_PER_PARTICLE = {"k_sweep_cl<3>": 168.5, "k_sweep<3>": 170.5}
+
+# FP32 instructions of one fluid-fluid pair of the fast sweep, counted from
+# the source of the clustered sweep's pair (separation 3, |r|^2 3, sqrt 1,
+# q 1, (2-q)^+ 2, powers 2, Shepard term 4, F factor 2, velocity difference
+# 3, (u_ij . r_ij) 3, pressure factor 2, grad p 3, lap u 3, div u 1, lap p
+# 2), a fused multiply-add counted once
+PAIR_FP32_INSTR = 37
+# FP32 lanes x SMs of one GB300 (the instruction rate of the FMA pipes at
+# the SM clock)
+FP32_LANES = 128 * 152
+
+
+def support_pairs(c, sample=40000, seed=0):
+    """Fluid-fluid pairs within the support (2H, j != i) per fluid particle,
+    counted with a k-d tree on a random sample of the fluid particles."""
+    from scipy.spatial import cKDTree
+    fl = np.flatnonzero(np.asarray(c.imove) == 1)
+    d = c.dims
+    pts = np.asarray(c.r, np.float64)[fl, :d]
+    tree = cKDTree(pts)
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(fl), size=min(sample, len(fl)), replace=False)
+    radius = float(c.params.SUPPORT) * float(c.params.H) * (1.0 - 1e-9)
+    cnt = tree.query_ball_point(pts[pick], radius, return_length=True)
+    return float(np.mean(cnt) - 1.0), len(fl)
 
 
 def load_traffic(kernel):
@@ -299,8 +325,8 @@ def workload_desc(name):
     if name == "c5":
         return (workload_desc("c4") + "; one step = one learned proposal of k=8 "
                 "plain steps (graph radius 0.9h: 26 lattice neighbours), "
-                "judged every proposal by the plain step over the whole field "
-                "(4 probes, density on a 10% fluid subsample)")
+                "judged every proposal by the plain rates on a 10% cell "
+                "sample (density residual, 4 probes)")
     d, n = WORKLOADS.get(name, WORKLOADS["c1"])
     return f"{d}: N={n}"
 
@@ -484,13 +510,34 @@ def run_ours(args):
     sweep_b = SWEEP_BYTES_3D if three_d else SWEEP_BYTES_2D
     step_b = STEP_BYTES_3D if three_d else STEP_BYTES_2D
     achieved = sweep_b * c.N / (stage_ms["sweep"] * 1e-3) / 1e9
-    traffic_pp = load_traffic("k_sweep<3>" if three_d else "k_sweep<2>")
-    roofline = {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved,
+    clustered = (three_d and args.precision == "fast" and
+                 (tuning is None or tuning["variant"] >= 15))
+    kname = ("k_sweep_cl" if clustered else "k_sweep") + ("<3>" if three_d else "<2>")
+    traffic_pp = load_traffic(kname)
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_src,
                 "traffic": traffic_pp * c.N if traffic_pp else None,
                 "algorithmic_bytes_per_launch": sweep_b * c.N}
     step_achieved = step_b * c.N / (ms_step * 1e-3) / 1e9
+    # the sweep is bound by instruction issue, not HBM: its useful FP32 work
+    # (in-support fluid pairs x the pair's FP32 instructions) against the
+    # FP32 lanes at the SM clock sampled during the timed steps
+    fp32_roofline = None
+    if rank == 0:
+        per, n_fl = support_pairs(c)
+        pairs = per * n_fl
+        mhz = (clk or {}).get("sm_mhz") or 2070.0
+        peak_ops = FP32_LANES * mhz * 1e6
+        ach = pairs * PAIR_FP32_INSTR / (stage_ms["sweep"] * 1e-3)
+        fp32_roofline = {"bound": "fp32 issue", "kernel": kname,
+                         "achieved": ach / 1e12, "peak": peak_ops / 1e12,
+                         "unit": "T instr/s", "frac": ach / peak_ops,
+                         "pairs_per_fluid_particle": per,
+                         "pair_fp32_instr": PAIR_FP32_INSTR,
+                         "note": "useful pair arithmetic only: the filter, "
+                                 "out-of-support lanes, staging and the "
+                                 "epilogue are the rest"}
 
     line = None
     if rank == 0:
@@ -524,6 +571,7 @@ def run_ours(args):
                     "steps": e2e_steps, "contexts": 2},
             "gpu_launches": sv.launches_per_step() * args.steps,
             "roofline": roofline,
+            "fp32_roofline": fp32_roofline,
             "step_roofline": {"bound": "hbm", "achieved": step_achieved,
                               "peak": peak, "unit": "GB/s",
                               "frac": step_achieved / peak,
@@ -540,18 +588,48 @@ def run_ours(args):
                 "t_max": max(k["t"] for k in ks),
                 "dt_min": min(k["dt"] for k in ks),
                 "dt_max": max(k["dt"] for k in ks)}
-        print(json.dumps(line), flush=True)
     sv.close()
+    if line is not None:
+        if args.workload == "c1" and world == 1 and not args.no_learned:
+            line["learned"] = learned_summary(args)
+        print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
 
 
-def run_learned(args):
+def learned_summary(args):
+    """The learned k = 8 proposal on the 64-tank sloshing batch with a
+    bounded training budget, for the default bench line: proposal
+    throughput against the plain step on the same batch, judge statistics
+    and the held-out gain of the trained network over extrapolation."""
+    la = argparse.Namespace(**vars(args))
+    la.train_pairs, la.train_iters = args.learned_pairs, args.learned_iters
+    la.steps, la.warmup, la.eval_warm = 5, 3, args.learned_warm
+    t0 = time.perf_counter()
+    try:
+        r = learned_c3(la)
+    except Exception as e:  # reported, not hidden: the line says what failed
+        return {"error": f"{type(e).__name__}: {e}"}
+    keys = ("metric", "value", "unit", "ms_per_step", "plain_value",
+            "learned_over_plain", "heldout_mse", "judge_stats", "e2e",
+            "roofline", "gpu_launches")
+    out = {k: r[k] for k in keys if k in r}
+    out["config"] = {"workload": r["config"]["workload"],
+                     "training": r["config"]["training"],
+                     "proposals_timed": la.steps,
+                     "plain_steps_before": la.eval_warm,
+                     "judge": r["config"]["judge"]}
+    out["wall_s"] = time.perf_counter() - t0
+    return out
+
+
+def learned_c3(args):
     """Learned k = 8 proposals with a plain judge on a quarter of the cases,
     on the 64-tank sloshing batch; the network is first trained on plain
-    trajectories of 32 other tanks drawn from the same distribution."""
+    trajectories of 32 other tanks drawn from the same distribution.
+    Returns the bench line."""
     import torch
     from aquagpusph_gb300 import case as cases
     from aquagpusph_gb300 import learned as Lm
@@ -716,15 +794,22 @@ def run_learned(args):
                      "traffic": None},
         "clocks": clk, "cpu_baseline": None,
     }
-    print(json.dumps(line), flush=True)
+    run.close()
     sv.close()
+    return line
+
+
+def run_learned(args):
+    print(json.dumps(learned_c3(args)), flush=True)
     return 0
 
 
 def run_learned_3d(args):
     """Learned k = 8 proposals on the 26M-particle 3-D dam break, each judged
-    by the plain step over the whole field; the network is first trained on
-    plain trajectories of a small dam break with the same dx, h and walls."""
+    by the plain rates at both ends on a 10% cell sample (and the cells
+    around the probes); a failed proposal is replaced by k plain steps.  The
+    network is first trained on plain trajectories of a small dam break with
+    the same dx, h and walls."""
     import torch
     from aquagpusph_gb300 import case as cases
     from aquagpusph_gb300 import learned as Lm
@@ -796,7 +881,9 @@ def run_learned_3d(args):
     dt_s = time.perf_counter() - t2
     clk = clocks.stop()
     calls = Lm.CALLS[0] - calls0
-    judge_launches = args.steps * K * run.judge.launches_per_step()
+    # two rate-sampled plain steps per proposal, k plain steps per rollback
+    judge_launches = (2 * args.steps * run.judge.launches_per_step() +
+                      st["rolled_back"] * K * sv.launches_per_step())
     value = c.N * K * args.steps / dt_s
     # the plain step on the same case, same number of particle-steps
     e0 = torch.cuda.Event(enable_timing=True)
@@ -836,7 +923,7 @@ def run_learned_3d(args):
     steps = args.steps
     line = {
         "metric": "particle-steps/s (learned k=8 proposal judged by the plain "
-                  "step over the whole field, 1 GB300)",
+                  "rates on a 10% cell sample, 1 GB300)",
         "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt_s / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -848,11 +935,15 @@ def run_learned_3d(args):
                        "pairs": args.train_pairs, "held_out": len(held),
                        "iterations": args.train_iters,
                        "train_s": train_s, "prep_s": prep_s},
-                   "judge": "plain k steps over the whole field every proposal; "
-                            "rollback of the whole field at > 2% probe-pressure "
-                            "error (of max(|p|, rho g 4h)) at any of the 4 "
-                            "probes or > 2% density error (of refd) on a 10% "
-                            "fluid subsample"},
+                   "judge": "every proposal: the plain rates (one plain "
+                            "step) at the start and the proposed state on a "
+                            "hashed 10% of the cells plus the cells around the "
+                            "4 probes; rollback (k plain steps from the start "
+                            "state) at > 2% density error (of refd) against "
+                            "the trapezoidal plain continuity equation on the "
+                            "sampled fluid, or > 2% probe-pressure error (of "
+                            "max(|p|, rho g 4h)) against the interpolation of "
+                            "those plain densities"},
         "plain_value": plain_value, "learned_over_plain": value / plain_value,
         "heldout_mse": {"trained": loss_trained,
                         "extrapolation_only": loss_zero},
@@ -957,6 +1048,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forward-only", action="store_true",
                     help="c3 / c5: time the network forward alone")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="c1: leave out the learned-proposal sub-object")
+    ap.add_argument("--learned-pairs", type=int, default=12)
+    ap.add_argument("--learned-iters", type=int, default=120)
+    ap.add_argument("--learned-warm", type=int, default=3000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

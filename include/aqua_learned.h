@@ -321,6 +321,24 @@ aqua_status aqua_gnn_sample_max_diff(uint32_t n, const float* a,
                                      const float* b, const int32_t* imove,
                                      uint32_t seed, float fraction, float scale,
                                      float* out, void* stream);
+/* The judge of a proposal on a rate sample (aqua_set_rate_sample with
+ * `fraction` and `seed`): a solver stepped once from the start state s0 and
+ * once from the proposed state s1 (k steps of dt later), each with the
+ * sample on, holds the plain rates drho/dt of the sampled cells at both
+ * ends.  For every particle, rho_judged[id] = rho0 + kdt/2 (drhodt0 +
+ * drhodt1): the density the plain continuity equation gives over the k
+ * steps (trapezoidal rule).  *out = max |rho1 - rho_judged| * scale over the
+ * fluid particles in sampled cells at both ends.  Inputs: id1, icell1 (cell
+ * keys), imove1, drhodt1 in the sorted order of the s1 step; icell0,
+ * drhodt0 of the s0 step and rho0, rho1 (s0, s1) by particle id; rho_judged
+ * by particle id. */
+aqua_status aqua_gnn_judge_density(uint32_t n, const uint32_t* id1,
+                                   const uint32_t* icell1, const int32_t* imove1,
+                                   const float* drhodt1, const uint32_t* icell0,
+                                   const float* drhodt0, const float* rho0,
+                                   const float* rho1, float kdt, float scale,
+                                   float fraction, uint32_t seed,
+                                   float* rho_judged, float* out, void* stream);
 /* out[c] = max over fluid particles i of case c of |a_i - b_i| * scale */
 aqua_status aqua_gnn_case_max_diff(uint32_t n_cases, const uint32_t* offsets,
                                    const float* a, const float* b,

@@ -75,4 +75,4 @@ def test_workload_table_is_shared_by_both_arms():
         assert desc == f"{d}: N={n}"
     assert bench.workload_desc("c3").startswith(bench.workload_desc("c2"))
     assert bench.workload_desc("c5").startswith(bench.workload_desc("c4"))
-    assert "whole field" in bench.workload_desc("c5")
+    assert "10% cell sample" in bench.workload_desc("c5")

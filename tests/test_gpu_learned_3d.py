@@ -1,5 +1,5 @@
-"""The learned proposal on one 3-D case, judged by the plain step over the
-whole field (FieldProposalRunner): the multi-probe pressure kernel against
+"""The learned proposal on one 3-D case, judged by the plain rates on a
+cell sample (FieldProposalRunner): the multi-probe pressure kernel against
 numpy, the 3-D network forward with the receiver sums fused in against the
 unfused kernels, training on a 3-D trajectory, and the accept / rollback
 decisions of the runner."""
@@ -172,7 +172,8 @@ def test_3d_training_and_fused_forward(torch):
 def test_field_runner_accepts_and_rolls_back(torch):
     """With an infinite tolerance every proposal stands (the resident state
     is the network's proposal and t advances by k dt); with a zero one every
-    proposal is rolled back to the plain field of the judge."""
+    proposal is rolled back: the resident state is then that of k plain
+    steps from the start state, bit for bit."""
     from aquagpusph_gb300 import learned as Lm
     from aquagpusph_gb300.solver import Solver
     c = small_3d()
@@ -184,6 +185,7 @@ def test_field_runner_accepts_and_rolls_back(torch):
         run = Lm.FieldProposalRunner(sv, c, model, k=8, tol=tol, seed=1)
         for _ in range(2):
             t0 = sv.scalars()
+            s0 = Lm.Snapshot.capture(sv, 3)
             p_err, rho_err, bad = run.advance()
             assert bad is expect_bad
             assert np.all(np.isfinite(p_err)) and len(p_err) == 2
@@ -191,20 +193,74 @@ def test_field_runner_accepts_and_rolls_back(torch):
             t1 = sv.scalars()
             assert t1["iter"] == t0["iter"] + 8
             if expect_bad:
-                js = run.judge.scalars()
-                assert t1["t"] == js["t"]
+                ref = Solver(c.params, capacity=c.N)
+                ref.set_state_raw(c.N, s0.ptrs(), False, t0["t"], t0["dt"],
+                                  t0["iter"])
+                ref.step(8, graph=True)
+                ref.check()
+                assert t1["t"] == ref.scalars()["t"]
                 mine = Lm.Snapshot.capture(sv, 3)
-                plain = Lm.Snapshot.capture(run.judge, 3)
+                plain = Lm.Snapshot.capture(ref, 3)
                 for f in ("r", "u", "rho"):
                     assert torch.equal(mine[f], plain[f]), f
+                ref.close()
             else:
                 assert abs(t1["t"] - (t0["t"] + 8 * t0["dt"])) <= 1e-6 * max(t1["t"], 1e-3)
         st = run.stats
         assert st["proposals"] == 2
         assert st["rolled_back"] == (2 if expect_bad else 0)
         assert st["n_edges"] > 0
+        assert "judge" in st["phase_s"]
         run.close()
         sv.close()
+
+
+def test_rate_sample_sweeps_only_its_cells(torch):
+    """aqua_set_rate_sample: a step from a state with dt = 0 leaves the
+    positions as they were, and with the sample on its rates equal the
+    full step's on the sampled cells and around the probes; the judge's
+    trapezoidal density of a state against itself (k dt = 0) is exact."""
+    from aquagpusph_gb300 import learned as Lm
+    from aquagpusph_gb300.solver import Solver
+    c = small_3d()
+    c.dt = c.params.dt_fixed
+    out = {}
+    for frac in (1.0, 0.3):
+        sv = Solver(c.params, capacity=c.N)
+        sv.set_precision(True)
+        sv.set_rate_sample(frac, 7)
+        sv.set_case(c)
+        sv.step(1, graph=False)
+        sv.check()
+        g = sv.get_case()
+        ex = sv.get_extra()
+        out[frac] = (g, ex["icell"])
+        sv.close()
+    full, _ = out[1.0]
+    samp, icell = out[0.3]
+    assert np.array_equal(full.id, samp.id)
+    h = np.array([_hash(int(k), 7) for k in icell], np.uint64)
+    sampled = h < int(0.3 * 2 ** 32)
+    fl = full.imove == 1
+    assert 0.1 < sampled[fl].mean() < 0.5
+    for f in ("dudt", "drhodt", "u", "rho", "r"):
+        a, b = getattr(full, f), getattr(samp, f)
+        assert np.array_equal(a[sampled & fl], b[sampled & fl]), f
+    # unsampled cells away from the probes keep the gather's values: some
+    # fluid rates differ from the full step's
+    assert not np.array_equal(full.drhodt[~sampled & fl], samp.drhodt[~sampled & fl])
+
+
+def _hash(key, seed):
+    """sample_hash of the library (aqua_internal.cuh), in Python."""
+    M = 0xFFFFFFFF
+    h = ((key * 0x9E3779B1) & M) ^ ((seed * 0x85EBCA77 + 0x165667B1) & M)
+    h ^= h >> 16
+    h = (h * 0x85EBCA6B) & M
+    h ^= h >> 13
+    h = (h * 0xC2B2AE35) & M
+    h ^= h >> 16
+    return h
 
 
 @pytest.mark.parametrize("dims", [2, 3])
