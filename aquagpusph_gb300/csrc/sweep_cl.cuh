@@ -636,10 +636,9 @@ k_sweep_cl(Consts c, StepArgs a)
                 uint16_t* list = S.list[warp];
                 uint16_t* wl = S.wall[warp];
 
-                // one fluid neighbour (staged slot j) of this lane's particle
-                auto fluid_pair = [&](uint32_t j) {
-                    const float4 pj = S.r0[j];
-                    const float4 vj = S.r1[j];
+                // one fluid neighbour (staged records pj, vj) of this lane's
+                // particle
+                auto fluid_pair = [&](const float4 pj, const float4 vj) {
                     const float d0 = pj.x - r0i.x, d1 = pj.y - r0i.y, d2 = pj.z - r0i.z;
                     const float rr = d0 * d0 + d1 * d1 + d2 * d2;
                     const float qq = sqrtf(rr) * c.inv_H;
@@ -662,10 +661,8 @@ k_sweep_cl(Consts c, StepArgs a)
                     du = du + udr * gf;
                     lp = lp + (vj.w - pi) * gf;
                 };
-                // one boundary element (staged slot j): BIe wall sums
-                auto wall_pair = [&](uint32_t j) {
-                    const float4 pj = S.r0[j];
-                    const float4 nj = S.r1[j];
+                // one boundary element (staged records pj, nj): BIe wall sums
+                auto wall_pair = [&](const float4 pj, const float4 nj) {
                     const float d0 = pj.x - r0i.x, d1 = pj.y - r0i.y, d2 = pj.z - r0i.z;
                     const float rr = d0 * d0 + d1 * d1 + d2 * d2;
                     const float qq = sqrtf(rr) * c.inv_H;
@@ -677,15 +674,22 @@ k_sweep_cl(Consts c, StepArgs a)
                     gw2 = gw2 + nj.z * wa;
                     dbi = dbi - nj.w * wa;
                 };
-                // sums the first nq quads of a list (lane takes slot q)
+                // sums the first nq quads of a list (lane takes slot q); the
+                // records of the next entry are loaded during this one's sums
                 auto drain = [&](const uint16_t* lst, uint32_t nq, bool walls) {
-#pragma unroll 2
+                    if (nq == 0)
+                        return;
+                    uint32_t j = lst[q];
+                    float4 a0 = S.r0[j], a1 = S.r1[j];
                     for (uint32_t t = 0; t < nq; t++) {
-                        const uint32_t j = lst[4 * t + q];
+                        const uint32_t jn = lst[4 * min(t + 1, nq - 1) + q];
+                        const float4 b0 = S.r0[jn], b1 = S.r1[jn];
                         if (walls)
-                            wall_pair(j);
+                            wall_pair(a0, a1);
                         else
-                            fluid_pair(j);
+                            fluid_pair(a0, a1);
+                        a0 = b0;
+                        a1 = b1;
                     }
                 };
 
@@ -746,21 +750,29 @@ k_sweep_cl(Consts c, StepArgs a)
                     }
                     uint32_t fill = 0;
                     uint32_t wdone = wfill;  // wall entries already summed
-                    for (uint32_t base = 0; base < nst; base += 32) {
-                        const uint32_t s = base + lane;
-                        bool f = false;
-                        if (s < nst) {
-                            const float4 pc = S.r0[s];
-                            const float bx = fmaxf(fabsf(pc.x - bc[0]) - be[0], 0.f);
-                            const float by = fmaxf(fabsf(pc.y - bc[1]) - be[1], 0.f);
-                            const float bz = fmaxf(fabsf(pc.z - bc[2]) - be[2], 0.f);
-                            f = (bx * bx + by * by + bz * bz < R2) && pc.w > 0.f;
-                        }
-                        const unsigned bf = __ballot_sync(0xffffffffu, f);
-                        if (f)
-                            list[fill + __popc(bf & lt)] = (uint16_t)s;
-                        fill += (uint32_t)__popc(bf);
-                        if (fill > (uint32_t)(kClListCap - 32)) {
+                    auto near_fluid = [&](uint32_t s) -> bool {
+                        if (s >= nst)
+                            return false;
+                        const float4 pc = S.r0[s];
+                        const float bx = fmaxf(fabsf(pc.x - bc[0]) - be[0], 0.f);
+                        const float by = fmaxf(fabsf(pc.y - bc[1]) - be[1], 0.f);
+                        const float bz = fmaxf(fabsf(pc.z - bc[2]) - be[2], 0.f);
+                        return (bx * bx + by * by + bz * bz < R2) && pc.w > 0.f;
+                    };
+                    // two independent rounds of 32 candidates per iteration
+                    for (uint32_t base = 0; base < nst; base += 64) {
+                        const uint32_t s0 = base + lane, s1 = base + 32 + lane;
+                        const bool f0 = near_fluid(s0);
+                        const bool f1 = near_fluid(s1);
+                        const unsigned b0 = __ballot_sync(0xffffffffu, f0);
+                        const unsigned b1 = __ballot_sync(0xffffffffu, f1);
+                        const uint32_t c0 = (uint32_t)__popc(b0);
+                        if (f0)
+                            list[fill + __popc(b0 & lt)] = (uint16_t)s0;
+                        if (f1)
+                            list[fill + c0 + __popc(b1 & lt)] = (uint16_t)s1;
+                        fill += c0 + (uint32_t)__popc(b1);
+                        if (fill > (uint32_t)(kClListCap - 64)) {
                             __syncwarp();
                             const uint32_t nq = fill / 4;
                             drain(list, nq, false);

@@ -606,7 +606,10 @@ def learned_summary(args):
     and the held-out gain of the trained network over extrapolation."""
     la = argparse.Namespace(**vars(args))
     la.train_pairs, la.train_iters = args.learned_pairs, args.learned_iters
+    # trained on and evaluated in the same regime: after learned_warm plain
+    # steps the sloshing has reached the left-wall probes
     la.steps, la.warmup, la.eval_warm = 5, 3, args.learned_warm
+    la.train_warm = args.learned_warm
     t0 = time.perf_counter()
     try:
         r = learned_c3(la)
@@ -639,7 +642,7 @@ def learned_c3(args):
     t0 = time.perf_counter()
     tb = cases.sloshing_batch_2d(n_cases=32, seed=1234)
     pairs, dts = Lm.collect_pairs(tb, K, n_pairs=args.train_pairs, gap=300,
-                                  warm=500)
+                                  warm=getattr(args, "train_warm", 500))
     model = Lm.Model(2, seed=0)
     Lm.fit_scales(model, pairs, dts, K, tb.case.params, Lm.case_ids(tb))
     sv_t = Solver(tb.case.params, capacity=tb.case.N)
@@ -765,6 +768,7 @@ def learned_c3(args):
                    "plain steps", "training": {
                        "tanks": "32 sloshing tanks, seed 1234 (config-2 distribution)",
                        "pairs": args.train_pairs, "iterations": args.train_iters,
+                       "first_pair_after_steps": getattr(args, "train_warm", 500),
                        "cases_per_step": 16, "train_s": train_s,
                        "prep_s": prep_s},
                    "judge": "plain step re-run of 25% of the cases; rollback at "
@@ -1050,9 +1054,11 @@ def main():
                     help="c3 / c5: time the network forward alone")
     ap.add_argument("--no-learned", action="store_true",
                     help="c1: leave out the learned-proposal sub-object")
-    ap.add_argument("--learned-pairs", type=int, default=12)
-    ap.add_argument("--learned-iters", type=int, default=120)
-    ap.add_argument("--learned-warm", type=int, default=3000)
+    ap.add_argument("--learned-pairs", type=int, default=24)
+    ap.add_argument("--learned-iters", type=int, default=300)
+    ap.add_argument("--learned-warm", type=int, default=20000)
+    ap.add_argument("--train-warm", type=int, default=500,
+                    help="c3: plain steps before the first training pair")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
