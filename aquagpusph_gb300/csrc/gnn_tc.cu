@@ -672,6 +672,295 @@ static_assert(edge_ctas_per_sm<true>() * (edge_mlp_smem<144>() + 1024) <= 228 * 
 static_assert(edge_ctas_per_sm<false>() * (edge_mlp_smem<16>() + 1024) <= 228 * 1024,
               "row-input CTAs per SM");
 
+
+// ---------------------------------------------------------------------------
+// Backward of a dense layer on the tensor cores (training).
+//
+// dgrad: dX = dY W, times silu'(Zprev) when the previous layer is SiLU.  It
+// is the forward's product with dY (M x N) as A and W^T (K x N, the
+// transposed weights kept by the model) as B: reduction over N (16 or 64),
+// K output columns (up to 160) in a tensor-memory accumulator of `tcols`
+// columns; the epilogue multiplies by silu'(Zprev) and rounds to BF16.
+//
+// wgrad: dW += dY^T X and db += column sums of dY.  The reduction runs over
+// the M rows (edges or nodes), 128 per chunk: each chunk of dY and X is
+// staged transposed (dY^T: N rows of 128, padded with zero rows to the
+// MMA's 128; X^T: K rows of 128) into the K-major core-matrix layout, and
+// the MMAs accumulate over all the CTA's chunks in tensor memory.  One
+// extra row of ones in B makes the column K of the product the column sums
+// of dY (db).  At the end each CTA adds its partial dW, db to the outputs
+// with atomics.
+
+__device__ __forceinline__ float
+silu_grad_f(float z)
+{
+    const float s = 1.f / (1.f + __expf(-z));
+    return s * (1.f + z * (1.f - s));
+}
+
+// bounded wait for a commit on `mbar` (phase parity `phase`); every thread
+// of the CTA returns the same verdict
+__device__ __forceinline__ bool
+tc_wait(uint64_t* mbar, uint32_t phase, uint32_t fake)
+{
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kWaitLimit && !done; it++) {
+        asm volatile("{\n.reg .pred p;\n"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     "selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(smem_addr(mbar)), "r"(phase));
+    }
+    // `fake` (test switch): a wait that completed counts as timed out
+    return !__syncthreads_or(!done || fake);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_linear_dgrad_tc(uint32_t M, uint32_t N, uint32_t K,
+                  const uint16_t* __restrict__ dY, uint32_t ldy,
+                  const uint16_t* __restrict__ Wt,
+                  const float* __restrict__ Zp, uint32_t ldzp, int act_prev,
+                  uint16_t* dX, uint32_t ldx, uint32_t tcols, int* err,
+                  uint32_t fake)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sB = smem;                                        // K x N
+    uint8_t* sA = smem + ((K * N * 2 + 1023) / 1024) * 1024;   // 128 x N
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    stage(sB, Wt, N, K, K, N);
+    if (threadIdx.x == 0)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n"
+                     :: "r"(smem_addr(&mbar)));
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 "
+                     "[%0], %1;\n" :: "r"(smem_addr(&tmem_base)), "r"(tcols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = make_idesc(K);
+    const uint32_t sbo = (N / 8) * 128;
+    uint32_t phase = 0;
+    const uint32_t tiles = (M + kTcRows - 1) / kTcRows;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t m0 = tile * kTcRows;
+        const uint32_t valid = min((uint32_t)kTcRows, M - m0);
+        stage(sA, dY + (size_t)m0 * ldy, ldy, kTcRows, valid, N);
+        asm volatile("fence.proxy.async.shared::cta;\n");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            for (uint32_t ks = 0; ks < N / 16; ks++) {
+                const uint64_t ad = make_desc(smem_addr(sA) + ks * 256, 128, sbo);
+                const uint64_t bd = make_desc(smem_addr(sB) + ks * 256, 128, sbo);
+                const uint32_t acc = ks > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                    :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one."
+                         "shared::cluster.b64 [%0];\n" :: "r"(smem_addr(&mbar)));
+        }
+        if (!tc_wait(&mbar, phase, fake)) {
+            if (threadIdx.x == 0)
+                atomicExch(err, 1);
+            tc_wait(&mbar, phase, 0u);  // the MMAs in flight, again bounded
+            break;
+        }
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        // epilogue: warp w owns rows 32w .. 32w + 31 (TMEM lanes)
+        const uint32_t row = m0 + warp * 32 + lane;
+        const uint32_t taddr = tmem + ((warp * 32u) << 16);
+        for (uint32_t c0 = 0; c0 < K; c0 += 16) {
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+                  "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+                  "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                  "=r"(v[14]), "=r"(v[15])
+                : "r"(taddr + c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+            if (row < M) {
+                float d[16];
+                for (int j = 0; j < 16; j++)
+                    d[j] = __uint_as_float(v[j]);
+                if (Zp && act_prev == AQUA_ACT_SILU) {
+                    const float* z = Zp + (size_t)row * ldzp + c0;
+                    for (int j = 0; j < 16; j += 4) {
+                        const float4 zz = *reinterpret_cast<const float4*>(z + j);
+                        d[j] *= silu_grad_f(zz.x);
+                        d[j + 1] *= silu_grad_f(zz.y);
+                        d[j + 2] *= silu_grad_f(zz.z);
+                        d[j + 3] *= silu_grad_f(zz.w);
+                    }
+                }
+                uint32_t pk[8];
+                for (int j = 0; j < 8; j++)
+                    pk[j] = pack2(d[2 * j], d[2 * j + 1]);
+                uint4* dst = reinterpret_cast<uint4*>(dX + (size_t)row * ldx + c0);
+                dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            }
+        }
+        // the next tile's MMAs overwrite the accumulator and sA
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncthreads();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n"
+                     :: "r"(tmem), "r"(tcols));
+    }
+}
+
+// rows x 128 transposed block: element (r, m) = src[m * ld + r] for r < nr
+// and m < valid, into the core-matrix layout with 128 columns (16 core
+// matrices along the reduction); rows >= nr are left as they are.  Two
+// consecutive m of one r form one 32-bit store.
+__device__ __forceinline__ void
+stage_t(uint8_t* dst, const uint16_t* src, uint32_t ld, uint32_t nr,
+        uint32_t valid)
+{
+    const uint32_t rg = nr / 8;  // 16-byte groups of a source row
+    for (uint32_t e = threadIdx.x; e < 64u * rg; e += kTcThreads) {
+        const uint32_t mp = e / rg, g = e % rg;  // row pair, column group
+        const uint32_t m = 2 * mp;
+        uint4 v0 = make_uint4(0, 0, 0, 0), v1 = make_uint4(0, 0, 0, 0);
+        if (m < valid)
+            v0 = *reinterpret_cast<const uint4*>(src + (size_t)m * ld + g * 8);
+        if (m + 1 < valid)
+            v1 = *reinterpret_cast<const uint4*>(src + (size_t)(m + 1) * ld + g * 8);
+        const uint32_t a0[4] = { v0.x, v0.y, v0.z, v0.w };
+        const uint32_t a1[4] = { v1.x, v1.y, v1.z, v1.w };
+        for (int j = 0; j < 8; j++) {
+            const uint32_t lo = (a0[j / 2] >> ((j & 1) * 16)) & 0xFFFFu;
+            const uint32_t hi = (a1[j / 2] >> ((j & 1) * 16)) & 0xFFFFu;
+            const uint32_t r = g * 8 + j;
+            *reinterpret_cast<uint32_t*>(
+                dst + ((r / 8) * 16 + m / 8) * 128 + (r % 8) * 16 + (m % 8) * 2) =
+                lo | (hi << 16);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_linear_wgrad_tc(uint32_t M, uint32_t N, uint32_t K,
+                  const uint16_t* __restrict__ dY, uint32_t ldy,
+                  const uint16_t* __restrict__ X, uint32_t ldx, float* dW,
+                  float* db, uint32_t KB, uint32_t tcols, int* err,
+                  uint32_t fake)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sA = smem;                  // 128 (N used) x 128: dY^T
+    uint8_t* sB = smem + 128 * 128 * 2;  // KB x 128: X^T, then ones, zeros
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t chunks = (M + kTcRows - 1) / kTcRows;
+    if ((uint32_t)blockIdx.x >= chunks)
+        return;  // no chunk for this CTA (before any allocation)
+    // rows N..127 of A stay zero; rows K..KB-1 of B: ones (db), then zeros
+    for (uint32_t e = threadIdx.x; e < 128u * 128u / 8u; e += kTcThreads)
+        reinterpret_cast<uint4*>(sA)[e] = make_uint4(0, 0, 0, 0);
+    for (uint32_t e = threadIdx.x; e < (KB - K) * 128u; e += kTcThreads) {
+        const uint32_t r = K + e / 128u, m = e % 128u;
+        const uint16_t one = (r == K && db) ? 0x3F80u : 0u;  // bf16 1.0
+        *reinterpret_cast<uint16_t*>(
+            sB + ((r / 8) * 16 + m / 8) * 128 + (r % 8) * 16 + (m % 8) * 2) = one;
+    }
+    if (threadIdx.x == 0)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n"
+                     :: "r"(smem_addr(&mbar)));
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 "
+                     "[%0], %1;\n" :: "r"(smem_addr(&tmem_base)), "r"(tcols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = make_idesc(KB);
+    constexpr uint32_t sbo = 16 * 128;  // 128 reduction columns per row group
+    uint32_t phase = 0;
+    bool failed = false, first = true;
+    for (uint32_t ch = blockIdx.x; ch < chunks; ch += gridDim.x) {
+        const uint32_t m0 = ch * kTcRows;
+        const uint32_t valid = min((uint32_t)kTcRows, M - m0);
+        stage_t(sA, dY + (size_t)m0 * ldy, ldy, N, valid);
+        stage_t(sB, X + (size_t)m0 * ldx, ldx, K, valid);
+        asm volatile("fence.proxy.async.shared::cta;\n");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            for (uint32_t ks = 0; ks < 8; ks++) {
+                const uint64_t ad = make_desc(smem_addr(sA) + ks * 256, 128, sbo);
+                const uint64_t bd = make_desc(smem_addr(sB) + ks * 256, 128, sbo);
+                const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                    :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one."
+                         "shared::cluster.b64 [%0];\n" :: "r"(smem_addr(&mbar)));
+        }
+        first = false;
+        // the MMAs read sA / sB: wait before the next chunk is staged
+        if (!tc_wait(&mbar, phase, fake)) {
+            failed = true;
+            tc_wait(&mbar, phase, 0u);  // the MMAs in flight, again bounded
+            break;
+        }
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+    }
+    if (failed) {
+        if (threadIdx.x == 0)
+            atomicExch(err, 1);
+    } else {
+        // epilogue: rows n = 32w + lane < N add their partial sums
+        const uint32_t n = warp * 32 + lane;
+        const uint32_t taddr = tmem + ((warp * 32u) << 16);
+        for (uint32_t c0 = 0; c0 < KB; c0 += 16) {
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+                  "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+                  "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                  "=r"(v[14]), "=r"(v[15])
+                : "r"(taddr + c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+            if (n < N) {
+                for (int j = 0; j < 16; j++) {
+                    const uint32_t col = c0 + j;
+                    if (col < K)
+                        atomicAdd(&dW[(size_t)n * K + col], __uint_as_float(v[j]));
+                    else if (col == K && db)
+                        atomicAdd(&db[n], __uint_as_float(v[j]));
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n"
+                     :: "r"(tmem), "r"(tcols));
+    }
+}
 }  // namespace
 
 namespace {
@@ -857,5 +1146,110 @@ aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N, const uint16_t* X,
     const uint32_t grid = tiles < (uint32_t)sms * 8u ? tiles : (uint32_t)sms * 8u;
     k_linear_fwd_tc<64><<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
         M, K, X, ldx, W, b, Z, ldz, Y, ldy, act, err, (uint32_t)aqua::g_debug_fake_timeout);
+    return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
+}
+
+namespace {
+
+// tensor-memory columns for an accumulator of `cols` columns (a power of 2,
+// at least 32), and the shared memory that keeps the CTAs of one SM within
+// its 512 columns, so that tcgen05.alloc never waits
+uint32_t
+tc_cols(uint32_t cols)
+{
+    uint32_t t = 32;
+    while (t < cols)
+        t *= 2;
+    return t;
+}
+
+size_t
+tc_min_smem(uint32_t tcols)
+{
+    return (size_t)233472 / (512u / tcols + 1u);
+}
+
+cudaError_t
+tc_sms(int* sms)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
+    return e;
+}
+
+bool
+al16(const void* p)
+{
+    return (reinterpret_cast<uintptr_t>(p) & 15) == 0;
+}
+
+}  // namespace
+
+extern "C" aqua_status
+aqua_gnn_linear_dgrad_tc(uint32_t M, uint32_t N, uint32_t K,
+                         const uint16_t* dY, uint32_t ldy, const uint16_t* Wt,
+                         const float* Zprev, uint32_t ldzp, int32_t act_prev,
+                         uint16_t* dX, uint32_t ldx, int32_t* err, void* stream)
+{
+    if (!dY || !Wt || !dX || !err || (N != 16 && N != 64) || K == 0 ||
+        K % 16 || K > 160 || ldy < N || ldy % 8 || ldx < K || ldx % 8 ||
+        !al16(dY) || !al16(Wt) || !al16(dX) ||
+        (Zprev && act_prev == AQUA_ACT_SILU &&
+         (ldzp < K || ldzp % 4 || !al16(Zprev))))
+        return AQUA_ERR_INVALID;
+    if (M == 0)
+        return AQUA_OK;
+    const uint32_t tcols = tc_cols(K);
+    size_t bytes = ((size_t)K * N * 2 + 1023) / 1024 * 1024 + (size_t)kTcRows * N * 2;
+    if (bytes < tc_min_smem(tcols))
+        bytes = tc_min_smem(tcols);
+    int sms = 0;
+    if (tc_sms(&sms) != cudaSuccess)
+        return AQUA_ERR_CUDA;
+    if (cudaFuncSetAttribute(k_linear_dgrad_tc,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes) != cudaSuccess)
+        return AQUA_ERR_CUDA;
+    const uint32_t tiles = (M + kTcRows - 1) / kTcRows;
+    const uint32_t cap = (uint32_t)sms * (512u / tcols);
+    const uint32_t grid = tiles < cap ? tiles : cap;
+    k_linear_dgrad_tc<<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
+        M, N, K, dY, ldy, Wt, Zprev, ldzp, act_prev, dX, ldx, tcols, err,
+        (uint32_t)aqua::g_debug_fake_timeout);
+    return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
+}
+
+extern "C" aqua_status
+aqua_gnn_linear_wgrad_tc(uint32_t M, uint32_t N, uint32_t K,
+                         const uint16_t* dY, uint32_t ldy, const uint16_t* X,
+                         uint32_t ldx, float* dW, float* db, int32_t* err,
+                         void* stream)
+{
+    if (!dY || !X || !dW || !err || (N != 16 && N != 64) || K == 0 ||
+        K % 16 || K > 160 || ldy < N || ldy % 8 || ldx < K || ldx % 8 ||
+        !al16(dY) || !al16(X))
+        return AQUA_ERR_INVALID;
+    if (M == 0)
+        return AQUA_OK;
+    const uint32_t KB = K + 16;  // + the row of ones (db) and zero padding
+    const uint32_t tcols = tc_cols(KB);
+    size_t bytes = (size_t)128 * 128 * 2 + (size_t)KB * 128 * 2;
+    if (bytes < tc_min_smem(tcols))
+        bytes = tc_min_smem(tcols);
+    int sms = 0;
+    if (tc_sms(&sms) != cudaSuccess)
+        return AQUA_ERR_CUDA;
+    if (cudaFuncSetAttribute(k_linear_wgrad_tc,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes) != cudaSuccess)
+        return AQUA_ERR_CUDA;
+    const uint32_t chunks = (M + kTcRows - 1) / kTcRows;
+    const uint32_t cap = (uint32_t)sms * (512u / tcols);
+    const uint32_t grid = chunks < cap ? chunks : cap;
+    k_linear_wgrad_tc<<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
+        M, N, K, dY, ldy, X, ldx, dW, db, KB, tcols, err,
+        (uint32_t)aqua::g_debug_fake_timeout);
     return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
 }

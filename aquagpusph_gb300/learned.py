@@ -109,6 +109,10 @@ SIGNATURES = {
                               _i32, _vp, _u32, _vp],
     "aqua_gnn_linear_wgrad": [_u32, _u32, _u32, _vp, _u32, _vp, _u32, _vp, _vp,
                               _vp],
+    "aqua_gnn_linear_dgrad_tc": [_u32, _u32, _u32, _vp, _u32, _vp, _vp, _u32,
+                                 _i32, _vp, _u32, _vp, _vp],
+    "aqua_gnn_linear_wgrad_tc": [_u32, _u32, _u32, _vp, _u32, _vp, _u32, _vp,
+                                 _vp, _vp, _vp],
     "aqua_gnn_segment_sum": [_u32, _vp, _vp, _u32, _f32, _vp, _u32, _u32, _vp],
     "aqua_gnn_segment_bcast": [_u32, _vp, _vp, _u32, _u32, _f32, _vp, _u32,
                                _vp],
@@ -566,15 +570,28 @@ class Network:
             name = f"{prefix}_{k}"
             o, ob, n, kk, act = m.offs[name]
             xin, ldin = ins[k]
-            _chk("aqua_gnn_linear_wgrad", L.aqua_gnn_linear_wgrad(
-                M, n, kk, _p(dY), n, xin, ldin, m.dW(name), m.db(name), s))
+            # weight and data gradients on the tensor cores (tcgen05) or on
+            # mma.sync
+            if self.tc:
+                _chk("aqua_gnn_linear_wgrad_tc", L.aqua_gnn_linear_wgrad_tc(
+                    M, n, kk, _p(dY), n, xin, ldin, m.dW(name), m.db(name),
+                    _p(self.err), s))
+            else:
+                _chk("aqua_gnn_linear_wgrad", L.aqua_gnn_linear_wgrad(
+                    M, n, kk, _p(dY), n, xin, ldin, m.dW(name), m.db(name), s))
             if k == 0 and not want_dx:
                 return None
             dX = self._buf((M, kk), torch.bfloat16)
             zp = _p(Z[k - 1]) if k > 0 else _vp(0)
-            _chk("aqua_gnn_linear_dgrad", L.aqua_gnn_linear_dgrad(
-                M, n, kk, _p(dY), n, _p(m.wt[name]), zp, kk if k > 0 else 0,
-                1 if k > 0 else 0, _p(dX), kk, s))
+            if self.tc:
+                _chk("aqua_gnn_linear_dgrad_tc", L.aqua_gnn_linear_dgrad_tc(
+                    M, n, kk, _p(dY), n, _p(m.wt[name]), zp,
+                    kk if k > 0 else 0, 1 if k > 0 else 0, _p(dX), kk,
+                    _p(self.err), s))
+            else:
+                _chk("aqua_gnn_linear_dgrad", L.aqua_gnn_linear_dgrad(
+                    M, n, kk, _p(dY), n, _p(m.wt[name]), zp,
+                    kk if k > 0 else 0, 1 if k > 0 else 0, _p(dX), kk, s))
             dY = dX
         return dY
 
@@ -605,6 +622,9 @@ class Network:
             E, _p(g.receivers), _p(dn1), 80, 0, AGG_SCALE, _p(dy), 64, s))
         A, Z = c["e1"]
         self._mlp_bwd("e1", _p(c["E0"]), FEAT, A, Z, dy, E, False)
+        if self.tc and int(self.err.item()):
+            raise _lib.AquaError("tensor-core backward (wait timed out)",
+                                 _lib.AQUA_ERR_CUDA)
 
 
 def mse_loss(out, target, mask, stream=None):

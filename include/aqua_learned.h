@@ -190,6 +190,27 @@ aqua_status aqua_gnn_linear_wgrad(uint32_t M, uint32_t N, uint32_t K,
                                   const uint16_t* X, uint32_t ldx, float* dW,
                                   float* db, void* stream);
 
+/* aqua_gnn_linear_dgrad on the 5th-generation tensor cores (tcgen05.mma,
+ * BF16 x BF16 -> FP32 in tensor memory): the same product and SiLU'
+ * epilogue; N in {16, 64}, K % 16 == 0, K <= 160; rows 16-byte aligned.
+ * A time-out of the bounded waits sets *err.  No counterpart in the
+ * reference. */
+aqua_status aqua_gnn_linear_dgrad_tc(uint32_t M, uint32_t N, uint32_t K,
+                                     const uint16_t* dY, uint32_t ldy,
+                                     const uint16_t* Wt, const float* Zprev,
+                                     uint32_t ldzp, int32_t act_prev,
+                                     uint16_t* dX, uint32_t ldx, int32_t* err,
+                                     void* stream);
+/* aqua_gnn_linear_wgrad on the tensor cores: dW += dY^T X (N x K f32) and
+ * db += column sums of dY (optional), the reduction over the M rows in
+ * chunks of 128 accumulated in tensor memory, then added with atomics;
+ * N in {16, 64}, K % 16 == 0, K <= 160.  A time-out sets *err. */
+aqua_status aqua_gnn_linear_wgrad_tc(uint32_t M, uint32_t N, uint32_t K,
+                                     const uint16_t* dY, uint32_t ldy,
+                                     const uint16_t* X, uint32_t ldx,
+                                     float* dW, float* db, int32_t* err,
+                                     void* stream);
+
 /* ---- graph aggregation ------------------------------------------------- */
 
 /* out[s] = scale * sum of Y rows of node s's edges (64 wide, bf16 out at

@@ -247,3 +247,58 @@ def test_fused_edge_mlp_sum_rejects_bad_arguments(torch):
         bad.append(a)
     for a in bad:
         assert L.aqua_gnn_edge_mlp_sum_tc(*a) == -1
+
+
+@pytest.mark.parametrize("M,N,K", [(1000, 64, 144), (300, 16, 64), (200000, 64, 64),
+                                   (1, 64, 80), (5000, 64, 16), (777, 16, 144)])
+def test_tcgen05_backward_matches(torch, M, N, K):
+    """The tensor-core backward of a dense layer (data gradient with the
+    SiLU' of the previous layer, weight and bias gradients) against numpy
+    (float64) and against the mma.sync kernels on the same BF16 inputs."""
+    from aquagpusph_gb300 import learned as Lm
+    L = Lm.lib()
+    rng = np.random.default_rng(M + 3 * N + 7 * K)
+    dY = G.bf16(rng.normal(0, 1, (M, N)).astype(np.float32))
+    W = G.bf16(rng.normal(0, 0.2, (N, K)).astype(np.float32))
+    X = G.bf16(rng.normal(0, 1, (M, K)).astype(np.float32))
+    Zp = rng.normal(0, 1.5, (M, K)).astype(np.float32)
+    dYd = torch.from_numpy(dY).cuda().to(torch.bfloat16)
+    Wtd = torch.from_numpy(np.ascontiguousarray(W.T)).cuda().to(torch.bfloat16)
+    Xd = torch.from_numpy(X).cuda().to(torch.bfloat16)
+    Zd = torch.from_numpy(Zp).cuda()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    # data gradient
+    dX1 = torch.empty((M, K), dtype=torch.bfloat16, device="cuda")
+    dX2 = torch.empty_like(dX1)
+    assert L.aqua_gnn_linear_dgrad_tc(M, N, K, Lm._p(dYd), N, Lm._p(Wtd),
+                                      Lm._p(Zd), K, 1, Lm._p(dX1), K,
+                                      Lm._p(err), None) == 0
+    assert L.aqua_gnn_linear_dgrad(M, N, K, Lm._p(dYd), N, Lm._p(Wtd),
+                                   Lm._p(Zd), K, 1, Lm._p(dX2), K, None) == 0
+    # weight and bias gradients (accumulated onto nonzero starting values)
+    dW0 = rng.normal(0, 1, (N, K)).astype(np.float32)
+    db0 = rng.normal(0, 1, N).astype(np.float32)
+    dW1, dW2 = torch.from_numpy(dW0).cuda(), torch.from_numpy(dW0).cuda()
+    db1, db2 = torch.from_numpy(db0).cuda(), torch.from_numpy(db0).cuda()
+    assert L.aqua_gnn_linear_wgrad_tc(M, N, K, Lm._p(dYd), N, Lm._p(Xd), K,
+                                      Lm._p(dW1), Lm._p(db1), Lm._p(err),
+                                      None) == 0
+    assert L.aqua_gnn_linear_wgrad(M, N, K, Lm._p(dYd), N, Lm._p(Xd), K,
+                                   Lm._p(dW2), Lm._p(db2), None) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    dy64, w64, x64, z64 = (a.astype(np.float64) for a in (dY, W, X, Zp))
+    sg = 1.0 / (1.0 + np.exp(-z64))
+    dx_ref = (dy64 @ w64) * sg * (1.0 + z64 * (1.0 - sg))
+    a1 = dX1.float().cpu().numpy()
+    a2 = dX2.float().cpu().numpy()
+    scale = max(np.abs(dx_ref).max(), 1e-30)
+    # one bf16 rounding of the output, plus f32 accumulation and SiLU'
+    assert np.abs(a1 - dx_ref).max() <= 2.0 ** -7 * scale
+    assert np.abs(a1 - a2).max() <= 2.0 ** -7 * scale
+    dw_ref = dW0 + dy64.T @ x64
+    db_ref = db0 + dy64.sum(0)
+    assert rel(dW1.cpu().numpy(), dw_ref) < 1e-5
+    assert rel(db1.cpu().numpy(), db_ref) < 1e-5
+    assert rel(dW1.cpu().numpy(), dW2.cpu().numpy()) < 1e-5
+    assert rel(db1.cpu().numpy(), db2.cpu().numpy()) < 1e-5
