@@ -823,63 +823,77 @@ k_linear_dgrad_tc(uint32_t M, uint32_t N, uint32_t K,
 }
 
 // rows x 128 transposed block: element (r, m) = src[m * ld + r] for r < nr
-// and m < valid, into the core-matrix layout with 128 columns (16 core
-// matrices along the reduction); rows >= nr are left as they are.  Two
-// consecutive m of one r form one 32-bit store.
+// and m < valid (zero for m >= valid), into the core-matrix layout with 128
+// reduction columns (16 core matrices per 8-row group); rows >= nr are left
+// as they are.  Each warp task moves four 8 x 8 blocks (four consecutive
+// 8-row groups of m, one 8-column group of r): every lane loads its
+// fragment element pair from global memory (row m = lane / 4, columns
+// 2 (lane % 4) and the next) and stmatrix .trans writes each block
+// transposed, whole 16-byte rows of a core matrix, free of bank conflicts.
 __device__ __forceinline__ void
 stage_t(uint8_t* dst, const uint16_t* src, uint32_t ld, uint32_t nr,
         uint32_t valid)
 {
-    const uint32_t rg = nr / 8;  // 16-byte groups of a source row
-    for (uint32_t e = threadIdx.x; e < 64u * rg; e += kTcThreads) {
-        const uint32_t mp = e / rg, g = e % rg;  // row pair, column group
-        const uint32_t m = 2 * mp;
-        uint4 v0 = make_uint4(0, 0, 0, 0), v1 = make_uint4(0, 0, 0, 0);
-        if (m < valid)
-            v0 = *reinterpret_cast<const uint4*>(src + (size_t)m * ld + g * 8);
-        if (m + 1 < valid)
-            v1 = *reinterpret_cast<const uint4*>(src + (size_t)(m + 1) * ld + g * 8);
-        const uint32_t a0[4] = { v0.x, v0.y, v0.z, v0.w };
-        const uint32_t a1[4] = { v1.x, v1.y, v1.z, v1.w };
-        for (int j = 0; j < 8; j++) {
-            const uint32_t lo = (a0[j / 2] >> ((j & 1) * 16)) & 0xFFFFu;
-            const uint32_t hi = (a1[j / 2] >> ((j & 1) * 16)) & 0xFFFFu;
-            const uint32_t r = g * 8 + j;
-            *reinterpret_cast<uint32_t*>(
-                dst + ((r / 8) * 16 + m / 8) * 128 + (r % 8) * 16 + (m % 8) * 2) =
-                lo | (hi << 16);
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rg = nr / 8;                        // 8-column groups of r
+    const uint32_t ar = lane >> 2, ac = (lane & 3) * 2;  // fragment position
+    const uint32_t mi = lane >> 3, mj = lane & 7;        // row address role
+    for (uint32_t t = warp; t < 4 * rg; t += blockDim.x / 32) {
+        const uint32_t mg = t & 3, kb = t >> 2;
+        uint32_t v[4];
+        for (int i = 0; i < 4; i++) {
+            const uint32_t m = (mg * 4 + i) * 8 + ar;
+            v[i] = m < valid ? *reinterpret_cast<const uint32_t*>(
+                                   src + (size_t)m * ld + kb * 8 + ac)
+                             : 0u;
         }
+        // lane 8i + j: row j of block i, stored transposed at the core
+        // matrix (r group kb, m group 4 mg + i)
+        const uint32_t addr =
+            smem_addr(dst + (kb * 16 + mg * 4 + mi) * 128 + mj * 16);
+        asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 "
+                     "[%0], {%1, %2, %3, %4};\n"
+                     :: "r"(addr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3])
+                     : "memory");
     }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+constexpr int kWgThreads = 256;  // wgrad: 8 warps stage, warps 0-3 read TMEM
+
+__global__ void __launch_bounds__(kWgThreads, 1)
 k_linear_wgrad_tc(uint32_t M, uint32_t N, uint32_t K,
                   const uint16_t* __restrict__ dY, uint32_t ldy,
                   const uint16_t* __restrict__ X, uint32_t ldx, float* dW,
-                  float* db, uint32_t KB, uint32_t tcols, int* err,
-                  uint32_t fake)
+                  float* db, uint32_t KB, uint32_t nbuf, uint32_t tcols,
+                  int* err, uint32_t fake)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
-    uint8_t* sA = smem;                  // 128 (N used) x 128: dY^T
-    uint8_t* sB = smem + 128 * 128 * 2;  // KB x 128: X^T, then ones, zeros
+    // nbuf (1 or 2) buffers, each A = dY^T (128 rows, N used) x 128 and
+    // B = X^T (KB rows: X^T, then the row of ones for db, then zeros) x 128;
+    // with two, a chunk is staged while the MMAs of the previous one run
+    const uint32_t bufb = 128 * 128 * 2 + KB * 128 * 2;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t chunks = (M + kTcRows - 1) / kTcRows;
     if ((uint32_t)blockIdx.x >= chunks)
         return;  // no chunk for this CTA (before any allocation)
-    // rows N..127 of A stay zero; rows K..KB-1 of B: ones (db), then zeros
-    for (uint32_t e = threadIdx.x; e < 128u * 128u / 8u; e += kTcThreads)
-        reinterpret_cast<uint4*>(sA)[e] = make_uint4(0, 0, 0, 0);
-    for (uint32_t e = threadIdx.x; e < (KB - K) * 128u; e += kTcThreads) {
-        const uint32_t r = K + e / 128u, m = e % 128u;
-        const uint16_t one = (r == K && db) ? 0x3F80u : 0u;  // bf16 1.0
-        *reinterpret_cast<uint16_t*>(
-            sB + ((r / 8) * 16 + m / 8) * 128 + (r % 8) * 16 + (m % 8) * 2) = one;
+    for (uint32_t b = 0; b < nbuf; b++) {
+        uint8_t* sA = smem + b * bufb;
+        uint8_t* sB = sA + 128 * 128 * 2;
+        for (uint32_t e = threadIdx.x; e < 128u * 128u / 8u; e += kWgThreads)
+            reinterpret_cast<uint4*>(sA)[e] = make_uint4(0, 0, 0, 0);
+        for (uint32_t e = threadIdx.x; e < (KB - K) * 128u; e += kWgThreads) {
+            const uint32_t r = K + e / 128u, m = e % 128u;
+            const uint16_t one = (r == K && db) ? 0x3F80u : 0u;  // bf16 1.0
+            *reinterpret_cast<uint16_t*>(
+                sB + ((r / 8) * 16 + m / 8) * 128 + (r % 8) * 16 + (m % 8) * 2) = one;
+        }
     }
     if (threadIdx.x == 0)
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n"
-                     :: "r"(smem_addr(&mbar)));
+        for (int b = 0; b < 2; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n"
+                         :: "r"(smem_addr(&mbar[b])));
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 "
                      "[%0], %1;\n" :: "r"(smem_addr(&tmem_base)), "r"(tcols));
@@ -891,9 +905,23 @@ k_linear_wgrad_tc(uint32_t M, uint32_t N, uint32_t K,
     const uint32_t tmem = tmem_base;
     const uint32_t idesc = make_idesc(KB);
     constexpr uint32_t sbo = 16 * 128;  // 128 reduction columns per row group
-    uint32_t phase = 0;
-    bool failed = false, first = true;
-    for (uint32_t ch = blockIdx.x; ch < chunks; ch += gridDim.x) {
+    uint32_t phase[2] = { 0u, 0u };
+    uint32_t pending[2] = { 0u, 0u };  // a commit of the buffer not yet waited
+    bool failed = false;
+    uint32_t it = 0;
+    for (uint32_t ch = blockIdx.x; ch < chunks && !failed; ch += gridDim.x, it++) {
+        const uint32_t b = it % nbuf;
+        uint8_t* sA = smem + b * bufb;
+        uint8_t* sB = sA + 128 * 128 * 2;
+        // the MMAs of the chunk nbuf ago read this buffer
+        if (pending[b]) {
+            if (!tc_wait(&mbar[b], phase[b], fake)) {
+                failed = true;
+                break;
+            }
+            phase[b] ^= 1u;
+            pending[b] = 0u;
+        }
         const uint32_t m0 = ch * kTcRows;
         const uint32_t valid = min((uint32_t)kTcRows, M - m0);
         stage_t(sA, dY + (size_t)m0 * ldy, ldy, N, valid);
@@ -905,29 +933,31 @@ k_linear_wgrad_tc(uint32_t M, uint32_t N, uint32_t K,
             for (uint32_t ks = 0; ks < 8; ks++) {
                 const uint64_t ad = make_desc(smem_addr(sA) + ks * 256, 128, sbo);
                 const uint64_t bd = make_desc(smem_addr(sB) + ks * 256, 128, sbo);
-                const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+                const uint32_t acc = (it == 0 && ks == 0) ? 0u : 1u;
                 asm volatile(
                     "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
                     :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one."
-                         "shared::cluster.b64 [%0];\n" :: "r"(smem_addr(&mbar)));
+                         "shared::cluster.b64 [%0];\n" :: "r"(smem_addr(&mbar[b])));
         }
-        first = false;
-        // the MMAs read sA / sB: wait before the next chunk is staged
-        if (!tc_wait(&mbar, phase, fake)) {
+        pending[b] = 1u;
+    }
+    // the last commits (the MMAs run in order: the later one covers both)
+    for (int b = 0; b < 2; b++) {
+        if (!pending[b])
+            continue;
+        if (!tc_wait(&mbar[b], phase[b], failed ? 0u : fake)) {
             failed = true;
-            tc_wait(&mbar, phase, 0u);  // the MMAs in flight, again bounded
-            break;
+            tc_wait(&mbar[b], phase[b], 0u);  // in flight, again bounded
         }
-        phase ^= 1u;
-        asm volatile("tcgen05.fence::after_thread_sync;\n");
     }
     if (failed) {
         if (threadIdx.x == 0)
             atomicExch(err, 1);
-    } else {
+    } else if (warp < 4) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
         // epilogue: rows n = 32w + lane < N add their partial sums
         const uint32_t n = warp * 32 + lane;
         const uint32_t taddr = tmem + ((warp * 32u) << 16);
@@ -1235,7 +1265,10 @@ aqua_gnn_linear_wgrad_tc(uint32_t M, uint32_t N, uint32_t K,
         return AQUA_OK;
     const uint32_t KB = K + 16;  // + the row of ones (db) and zero padding
     const uint32_t tcols = tc_cols(KB);
-    size_t bytes = (size_t)128 * 128 * 2 + (size_t)KB * 128 * 2;
+    const size_t buf = (size_t)128 * 128 * 2 + (size_t)KB * 128 * 2;
+    // two staging buffers where two CTAs per SM still fit, else one
+    const uint32_t nbuf = 233472 / (2 * buf + 1024) >= 2 ? 2u : 1u;
+    size_t bytes = nbuf * buf;
     if (bytes < tc_min_smem(tcols))
         bytes = tc_min_smem(tcols);
     int sms = 0;
@@ -1246,10 +1279,15 @@ aqua_gnn_linear_wgrad_tc(uint32_t M, uint32_t N, uint32_t K,
                              (int)bytes) != cudaSuccess)
         return AQUA_ERR_CUDA;
     const uint32_t chunks = (M + kTcRows - 1) / kTcRows;
-    const uint32_t cap = (uint32_t)sms * (512u / tcols);
+    // CTAs resident per SM: tensor-memory columns and shared memory
+    uint32_t per_sm = 512u / tcols;
+    const uint32_t by_smem = (uint32_t)(233472 / (bytes + 1024));
+    if (by_smem < per_sm)
+        per_sm = by_smem;
+    const uint32_t cap = (uint32_t)sms * (per_sm > 0 ? per_sm : 1u);
     const uint32_t grid = chunks < cap ? chunks : cap;
-    k_linear_wgrad_tc<<<grid, kTcThreads, bytes, (cudaStream_t)stream>>>(
-        M, N, K, dY, ldy, X, ldx, dW, db, KB, tcols, err,
+    k_linear_wgrad_tc<<<grid, kWgThreads, bytes, (cudaStream_t)stream>>>(
+        M, N, K, dY, ldy, X, ldx, dW, db, KB, nbuf, tcols, err,
         (uint32_t)aqua::g_debug_fake_timeout);
     return cudaGetLastError() == cudaSuccess ? AQUA_OK : AQUA_ERR_CUDA;
 }
