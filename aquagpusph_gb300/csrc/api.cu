@@ -219,13 +219,11 @@ layout(aqua_ctx* x, char* base)
         v.p = cv.take<float>(n);
     }
     StepBufs& b = x->b;
-    const uint32_t nb = sort_blocks(n > 0 ? n : 1);
     for (int k = 0; k < 2; k++) {
         b.keys[k] = cv.take<uint32_t>(n);
         b.vals[k] = cv.take<uint32_t>(n);
     }
-    b.counts = cv.take<uint32_t>((size_t)256 * nb);
-    b.digit_total = cv.take<uint32_t>(256);
+    b.sort_scratch = cv.take<uint32_t>(sort_scratch_words(n > 0 ? n : 1));
     b.cells = cv.take<uint2>(x->ncap);
     b.chunks = cv.take<uint2>(n);
     b.wall_range = cv.take<uint2>(x->ncap);
@@ -331,21 +329,25 @@ enqueue_step(aqua_ctx* x, int cur, cudaStream_t s)
     AQ_CUDA(launch_begin(x->sc, x->cs, x->n_cases, b.cells, b.wall_range,
                          x->consts.sample_on ? b.cell_mark : nullptr, x->ncap,
                          N, s));
+    // one case: every particle's case id is 0 (not read)
+    const uint32_t* cid = x->n_cases > 1 ? S.cid : nullptr;
     if (x->dims == 3) {
-        AQ_CUDA(launch_minmax<3>(x->consts, S.r, S.imove, S.cid, N, x->cs,
+        AQ_CUDA(launch_minmax<3>(x->consts, S.r, S.imove, cid, N, x->cs,
                                  x->sc, s));
         AQ_CUDA(launch_ncells<3>(x->consts, x->cs, x->n_cases, x->sc, x->ncap, s));
-        AQ_CUDA(launch_icell_hist<3>(x->consts, S.r, S.imove, S.cid, N, x->cs,
-                                     x->sc, b.keys[0], b.vals[0], b.counts, s));
+        AQ_CUDA(launch_icell_hist<3>(x->consts, S.r, S.imove, cid, N, x->cs,
+                                     x->sc, b.keys[0], b.sort_scratch,
+                                     x->passes, s));
     } else {
-        AQ_CUDA(launch_minmax<2>(x->consts, S.r, S.imove, S.cid, N, x->cs,
+        AQ_CUDA(launch_minmax<2>(x->consts, S.r, S.imove, cid, N, x->cs,
                                  x->sc, s));
         AQ_CUDA(launch_ncells<2>(x->consts, x->cs, x->n_cases, x->sc, x->ncap, s));
-        AQ_CUDA(launch_icell_hist<2>(x->consts, S.r, S.imove, S.cid, N, x->cs,
-                                     x->sc, b.keys[0], b.vals[0], b.counts, s));
+        AQ_CUDA(launch_icell_hist<2>(x->consts, S.r, S.imove, cid, N, x->cs,
+                                     x->sc, b.keys[0], b.sort_scratch,
+                                     x->passes, s));
     }
-    AQ_CUDA(launch_radix_passes(b.keys, b.vals, N, x->passes, b.counts,
-                                b.digit_total, true, x->sc, s));
+    AQ_CUDA(launch_radix_passes(b.keys, b.vals, N, x->passes, b.sort_scratch,
+                                true, x->sc, s));
     StepArgs a;
     a.N = N;
     a.ncap = x->ncap;
@@ -993,9 +995,8 @@ aqua_radix_sort(aqua_ctx* x, uint32_t* keys, uint32_t* perm, uint32_t* inv_perm,
     StepBufs& b = x->b;
     const uint32_t passes = sort_passes(key_bits);
     AQ_CUDA(cudaMemcpyAsync(b.keys[0], keys, n * 4ull, cudaMemcpyDeviceToDevice, s));
-    AQ_CUDA(launch_iota(b.vals[0], n, s));
-    AQ_CUDA(launch_radix_passes(b.keys, b.vals, n, passes, b.counts,
-                                b.digit_total, false, nullptr, s));
+    AQ_CUDA(launch_radix_passes(b.keys, b.vals, n, passes, b.sort_scratch,
+                                false, x->sc_aux, s));
     const int r = passes & 1;
     AQ_CUDA(cudaMemcpyAsync(keys, b.keys[r], n * 4ull, cudaMemcpyDeviceToDevice, s));
     if (perm)
@@ -1017,6 +1018,7 @@ aqua_linklist(aqua_ctx* x, const float* r_in, uint32_t N, uint32_t* icell,
     cudaStream_t s = (cudaStream_t)stream;
     StepBufs& b = x->b;
     const uint32_t ncap = ihoc_capacity < x->ncap ? ihoc_capacity : x->ncap;
+    const uint32_t passes = sort_passes(bits_for(ncap));
     DevScalars hs;
     std::memset(&hs, 0, sizeof(hs));
     AQ_CUDA(cudaMemcpyAsync(x->sc_aux, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
@@ -1027,19 +1029,18 @@ aqua_linklist(aqua_ctx* x, const float* r_in, uint32_t N, uint32_t* icell,
                                  x->sc_aux, s));
         AQ_CUDA(launch_ncells<3>(x->consts, x->cs_aux, 1, x->sc_aux, ncap, s));
         AQ_CUDA(launch_icell_hist<3>(x->consts, r_in, nullptr, nullptr, N,
-                                     x->cs_aux, x->sc_aux, b.keys[0], b.vals[0],
-                                     b.counts, s));
+                                     x->cs_aux, x->sc_aux, b.keys[0],
+                                     b.sort_scratch, passes, s));
     } else {
         AQ_CUDA(launch_minmax<2>(x->consts, r_in, nullptr, nullptr, N, x->cs_aux,
                                  x->sc_aux, s));
         AQ_CUDA(launch_ncells<2>(x->consts, x->cs_aux, 1, x->sc_aux, ncap, s));
         AQ_CUDA(launch_icell_hist<2>(x->consts, r_in, nullptr, nullptr, N,
-                                     x->cs_aux, x->sc_aux, b.keys[0], b.vals[0],
-                                     b.counts, s));
+                                     x->cs_aux, x->sc_aux, b.keys[0],
+                                     b.sort_scratch, passes, s));
     }
-    const uint32_t passes = sort_passes(bits_for(ncap));
-    AQ_CUDA(launch_radix_passes(b.keys, b.vals, N, passes, b.counts,
-                                b.digit_total, true, x->sc_aux, s));
+    AQ_CUDA(launch_radix_passes(b.keys, b.vals, N, passes, b.sort_scratch,
+                                true, x->sc_aux, s));
     const int r = passes & 1;
     AQ_CUDA(cudaMemcpyAsync(icell, b.keys[r], N * 4ull, cudaMemcpyDeviceToDevice, s));
     if (id_unsorted)
@@ -1116,9 +1117,10 @@ aqua_launches_per_step(aqua_ctx* x)
     if (!x)
         return 0;
     // begin, minmax, ncells, icell+hist, (passes - 1) hist,
-    // passes x (scan, scatter), gather, [BI walls,] chunks or clusters,
-    // sweep, finalize [, motion]
+    // passes x (scan, scatter), gather, [BI walls,] chunks or (cell list,
+    // clusters), sweep, finalize [, motion]
     return 4u + (x->passes - 1u) + 2u * x->passes + 4u +
+           (sweep_clustered(x) ? 1u : 0u) +
            (x->consts.boundary == AQUA_BOUNDARY_BI ? 1u : 0u) +
            (x->has_motion ? 1u : 0u);
 }

@@ -115,8 +115,7 @@ struct DevScalars
     uint32_t n_chunks;    // cell-aligned sweep chunks of this step
     uint32_t chunk_next;  // next chunk to hand out (work counter)
     uint32_t total_cells; // cells of all cases
-    uint32_t n_clusters;  // particle clusters of the clustered sweep
-    uint32_t pad[3];
+    uint32_t pad[4];
 };
 
 // One set of the per-particle Variables (reference layout)
@@ -144,8 +143,8 @@ struct StepBufs
     // link-list
     uint32_t* keys[2];     // radix ping-pong keys
     uint32_t* vals[2];     // radix ping-pong values (original index)
-    uint32_t* counts;      // per-pass digit x block counts
-    uint32_t* digit_total; // per-pass digit totals (256)
+    uint32_t* sort_scratch; // digit histograms, tile counters, look-back
+                            // status (sort_scratch_words)
     uint2* cells;          // (start, end) per cell; (N, N) if empty
     uint2* chunks;         // (first, count) sweep chunks (<= N)
     uint2* wall_range;     // first and one past the last sorted index of the

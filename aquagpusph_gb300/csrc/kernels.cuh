@@ -99,16 +99,19 @@ cudaError_t launch_minmax(const Consts& c, const float* r, const int32_t* imove,
 template<int D>
 cudaError_t launch_ncells(const Consts& c, CaseScalars* cs, uint32_t n_cases,
                           DevScalars* sc, uint32_t ncap, cudaStream_t s);
+// icell keys of the positions and the digit histograms (resets the sort
+// scratch first); then launch_radix_passes(..., hist_ready = true)
 template<int D>
 cudaError_t launch_icell_hist(const Consts& c, const float* r,
                               const int32_t* imove, const uint32_t* cid,
                               uint32_t N, const CaseScalars* cs, DevScalars* sc,
-                              uint32_t* keys, uint32_t* vals, uint32_t* counts,
-                              cudaStream_t s);
+                              uint32_t* keys, uint32_t* scratch,
+                              uint32_t passes, cudaStream_t s);
 cudaError_t launch_radix_passes(uint32_t* keys[2], uint32_t* vals[2],
-                                uint32_t n, uint32_t passes, uint32_t* counts,
-                                uint32_t* digit_total, bool first_counts_ready,
-                                const DevScalars* sc, cudaStream_t s);
+                                uint32_t n, uint32_t passes, uint32_t* scratch,
+                                bool hist_ready, DevScalars* sc,
+                                cudaStream_t s);
+size_t sort_scratch_words(uint32_t n);
 cudaError_t launch_inverse_perm(const uint32_t* perm, uint32_t* inv,
                                 uint32_t n, const DevScalars* sc,
                                 cudaStream_t s);

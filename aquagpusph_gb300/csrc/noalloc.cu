@@ -41,8 +41,11 @@ namespace {
 
 constexpr uint32_t kMaxKeys = AQUA_NOALLOC_SORT_MAX_KEYS;
 constexpr uint32_t kMaxBlocks = (kMaxKeys + kSortTile - 1) / kSortTile;
-// keys ping-pong partner, values ping-pong pair, per-pass counts, totals
-constexpr size_t kWords = 3ull * kMaxKeys + 256ull * kMaxBlocks + 256ull;
+// keys ping-pong partner, values ping-pong pair, the sort scratch (digit
+// histograms and counters: 1,056 words; two look-back status arrays of 256
+// words per tile)
+constexpr size_t kSortWords = 4ull * 256ull + 32ull + 2ull * 256ull * kMaxBlocks;
+constexpr size_t kWords = 3ull * kMaxKeys + kSortWords;
 
 static __device__ __align__(256) uint32_t g_sort_scratch[kWords];
 
@@ -169,12 +172,12 @@ aqua_radix_sort_noalloc(uint32_t* keys, uint32_t* perm, uint32_t* inv_perm,
     // the caller's keys are one half of the key ping-pong (sorted in place)
     uint32_t* kbuf[2] = { keys, base };
     uint32_t* vbuf[2] = { base + kMaxKeys, base + 2ull * kMaxKeys };
-    uint32_t* counts = base + 3ull * kMaxKeys;
-    uint32_t* digit_total = counts + 256ull * kMaxBlocks;
+    uint32_t* sort_scratch = base + 3ull * kMaxKeys;
     const uint32_t passes = sort_passes(key_bits);
-    NA_CUDA(launch_iota(vbuf[0], n, s));
-    NA_CUDA(launch_radix_passes(kbuf, vbuf, n, passes, counts, digit_total,
-                                false, nullptr, s));
+    if (sort_scratch_words(n) > kSortWords)
+        return AQUA_ERR_CAPACITY;
+    NA_CUDA(launch_radix_passes(kbuf, vbuf, n, passes, sort_scratch, false,
+                                nullptr, s));
     const int r = passes & 1;
     if (r)
         NA_CUDA(cudaMemcpyAsync(keys, kbuf[1], n * 4ull,

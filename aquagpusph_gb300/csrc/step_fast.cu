@@ -20,6 +20,9 @@ cudaError_t
 launch_cl(const Consts& c, const StepArgs& a, unsigned grid, unsigned sms,
           cudaStream_t s)
 {
+    constexpr uint32_t kPer = kCellListThreads * kCellListItems;
+    k_cell_list<<<max(1u, (a.N + kPer - 1) / kPer), kCellListThreads, 0, s>>>(
+        a.skeys, a.N, a.b.work, a.sc);
     k_clusters<<<sms * 8u, 256, 0, s>>>(c, a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)

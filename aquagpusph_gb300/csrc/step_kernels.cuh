@@ -259,22 +259,8 @@ k_gather(Consts c, StepArgs a)
     }
     const uint32_t o = a.perm[s];
     a.b.id_sorted[o] = s;
-    const bool cell_start = s == 0 || a.skeys[s - 1] != key;
-    if (cell_start)
+    if (s == 0 || a.skeys[s - 1] != key)
         a.b.cells[key].x = s;
-    if (a.clustered) {
-        // the list of cells holding particles (one entry per cell start),
-        // one atomic per warp
-        const unsigned act = __activemask();
-        const unsigned b = __ballot_sync(act, cell_start);
-        const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
-        uint32_t base = 0;
-        if (lane == leader && b)
-            base = atomicAdd(&a.sc->n_chunks, (uint32_t)__popc(b));
-        base = __shfl_sync(act, base, leader);
-        if (cell_start)
-            a.b.work[base + __popc(b & ((1u << lane) - 1u))] = make_uint2(key, s);
-    }
     if (s == N - 1 || a.skeys[s + 1] != key)
         a.b.cells[key].y = s + 1;
 
@@ -367,13 +353,20 @@ k_gather(Consts c, StepArgs a)
     else
         p = S.p[s];  // the pressure Variable is not permuted by the sort
 
-    Vec<D>::store(T.r, s, r);
+    // The clustered sweep (fast 3-D build, midpoint scheme, every cell
+    // swept) writes r, u, dudt, drhodt and rho of every fluid particle and
+    // reads none of them before: the gather leaves them out there.
+    const bool swept = a.clustered && !c.sample_on && !heun && im == 1;
+    if (!swept) {
+        Vec<D>::store(T.r, s, r);
+        Vec<D>::store(T.u, s, uh);
+    }
     Vec<D>::store(a.b.r_in, s, r);
-    Vec<D>::store(T.u, s, uh);
     Vec<D>::store(a.b.u_in, s, uin);
     Vec<D>::store(a.b.dudt_in, s, ain);
     a.b.drhodt_in[s] = drhodt_in;
-    if (heun) {
+    if (swept) {
+    } else if (heun) {
         // Without the midpoint init copies nothing permutes the rates
         // Variables: until the rates are computed (fluid only, cfd/Rates.cl)
         // dudt and drhodt keep the last step's order, and BI/GradP.cl reads
@@ -386,7 +379,8 @@ k_gather(Consts c, StepArgs a)
         Vec<D>::store(T.dudt, s, ain);
         T.drhodt[s] = drhodt_in;
     }
-    T.rho[s] = rho_h;
+    if (!swept)
+        T.rho[s] = rho_h;
     a.b.rho_in[s] = rho_in;
     T.m[s] = m;
     T.p[s] = p;

@@ -15,7 +15,9 @@
 // Clusters: k_clusters groups each cell's particles by octant into
 // clusters of at most 8 (small octant groups merge).  A warp takes one
 // cluster at a time as 8 particles x 4 neighbour slots: lane l holds
-// particle l / 4 and takes every fourth neighbour of the cluster's list.
+// particle l % 8 and takes every fourth neighbour of the cluster's list from
+// slot l / 8 on, so that the 8 lanes of one phase of a 16-byte shared load
+// read the same record (a broadcast, free of bank conflicts).
 // The list holds the staged candidates within the support of the
 // cluster's bounding box (a lane-parallel filter over the staged records,
 // compacted with ballots), so about 60% of the evaluated pairs lie in the
@@ -72,6 +74,60 @@ struct ClSmem
     uint32_t work;
     uint64_t mbar;
 };
+
+// The cells holding particles, as (key, first sorted index): position s
+// starts a cell where the sorted key changes.  A block takes
+// kCellListThreads x kCellListItems positions and reserves its entries with
+// one atomicAdd (the order of the list does not matter: every cell is swept
+// the same wherever it sits in it).
+constexpr int kCellListThreads = 1024;
+constexpr int kCellListItems = 8;
+__global__ void __launch_bounds__(kCellListThreads)
+k_cell_list(const uint32_t* skeys, uint32_t N, uint2* work, DevScalars* sc)
+{
+    __shared__ uint32_t s_warp[kCellListThreads / 32];
+    __shared__ uint32_t s_base;
+    if (__syncthreads_or(threadIdx.x == 0 && sc->err))
+        return;  // one read for the whole block
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t base = blockIdx.x * (uint32_t)(kCellListThreads * kCellListItems);
+    uint32_t starts = 0;  // bit it: position base + it * threads + t starts a cell
+    for (int it = 0; it < kCellListItems; it++) {
+        const uint32_t s = base + it * kCellListThreads + threadIdx.x;
+        if (s < N && (s == 0 || skeys[s - 1] != skeys[s]))
+            starts |= 1u << it;
+    }
+    // block-wide exclusive scan of the counts
+    const uint32_t v = (uint32_t)__popc(starts);
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = s_warp[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o)
+                w += y;
+        }
+        s_warp[lane] = w;  // inclusive warp totals
+        if (lane == 31)
+            s_base = w ? atomicAdd(&sc->n_chunks, w) : 0u;
+    }
+    __syncthreads();
+    uint32_t o = s_base + (warp > 0 ? s_warp[warp - 1] : 0u) + x - v;
+    for (int it = 0; it < kCellListItems; it++) {
+        if (starts & (1u << it)) {
+            const uint32_t s = base + it * kCellListThreads + threadIdx.x;
+            work[o++] = make_uint2(skeys[s], s);
+        }
+    }
+}
 
 // Clusters of every cell in the work list: one warp per cell.  The cell's
 // particles are ordered by group (octants 0-7 of the cell, then probes) into
@@ -157,10 +213,8 @@ k_clusters(Consts c, StepArgs a)
                 }
                 return k;
             };
-            const uint32_t n_cl = walk(false, 0);
-            const uint32_t base = atomicAdd(&a.sc->n_clusters, n_cl);
-            walk(true, base);
-            a.b.wcl[w] = make_uint4(first, end, base, n_cl);
+            const uint32_t n_cl = walk(true, first) - first;
+            a.b.wcl[w] = make_uint4(first, end, first, n_cl);
         }
         __syncwarp();
         if (lane < 16)
@@ -206,12 +260,28 @@ sweep_cl_finish(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
         return INFINITY;
     const VarSet& T = a.dst;
     const float hdt = 0.5f * dt;
-    const float rho_i = T.rho[i];
     const float p_i = r1i.w;
     if (store && a.b.shepard)
         a.b.shepard[i] = want ? shep : 0.f;
-    const float4 u4 = reinterpret_cast<const float4*>(T.u)[i];
-    const float ui_full[4] = { u4.x, u4.y, u4.z, u4.w };
+    float ain[4], uin[4];
+    Vec<3>::load(a.b.dudt_in, i, ain);
+    Vec<3>::load(a.b.u_in, i, uin);
+    const float drhodt_in = a.b.drhodt_in[i];
+    // the midpoint density and velocity of k_gather: recomputed for fluid
+    // (the gather leaves T.rho and T.u to this epilogue), read otherwise
+    float rho_i, ui_full[4];
+    if (fluid) {
+        rho_i = a.b.rho_in[i] + hdt * drhodt_in;
+        for (int k = 0; k < 4; k++)
+            ui_full[k] = uin[k] + hdt * ain[k];
+    } else {
+        rho_i = T.rho[i];
+        const float4 u4 = reinterpret_cast<const float4*>(T.u)[i];
+        ui_full[0] = u4.x;
+        ui_full[1] = u4.y;
+        ui_full[2] = u4.z;
+        ui_full[3] = u4.w;
+    }
     float gpf[4] = { 0.f, 0.f, 0.f, 0.f }, luf[4] = { 0.f, 0.f, 0.f, 0.f };
     float gwf[4] = { 0.f, 0.f, 0.f, 0.f };
     float div_u = 0.f;
@@ -295,10 +365,6 @@ sweep_cl_finish(const Consts& c, const StepArgs& a, uint32_t i, bool valid,
     const uint32_t set = set_raw < c.n_sets ? set_raw : 0u;
     float acc[4];
     float drhodt;
-    float ain[4], uin[4];
-    Vec<3>::load(a.b.dudt_in, i, ain);
-    Vec<3>::load(a.b.u_in, i, uin);
-    const float drhodt_in = a.b.drhodt_in[i];
     const float ri[3] = { r0i.x, r0i.y, r0i.z };
     if (fluid) {
         // cfd Rates.cl + deltaSPH
@@ -421,8 +487,8 @@ k_sweep_cl(Consts c, StepArgs a)
     extern __shared__ __align__(128) uint8_t smem_raw[];
     ClSmem<NW, CAP>& S = *reinterpret_cast<ClSmem<NW, CAP>*>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int q = lane & 3;          // neighbour slot
-    const int mq = lane >> 2;        // particle of the cluster
+    const int q = lane >> 3;         // neighbour slot (lanes 8 q .. 8 q + 7)
+    const int mq = lane & 7;         // particle of the cluster
     const uint32_t lt = (1u << lane) - 1u;
     const VarSet& T = a.dst;
     if (tid == 0) {
@@ -847,8 +913,8 @@ k_sweep_cl(Consts c, StepArgs a)
 #pragma unroll
                     for (int k = 0; k < 13; k++) {
                         float v = *acc[k];
-                        v = v + __shfl_xor_sync(0xffffffffu, v, 1);
-                        v = v + __shfl_xor_sync(0xffffffffu, v, 2);
+                        v = v + __shfl_xor_sync(0xffffffffu, v, 8);
+                        v = v + __shfl_xor_sync(0xffffffffu, v, 16);
                         *acc[k] = v;
                     }
                     const float v = sweep_cl_finish(

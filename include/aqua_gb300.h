@@ -335,8 +335,9 @@ aqua_status aqua_debug_fake_timeouts(int on);
  * loop, code running while a stream is captured, a process held to a fixed
  * device-memory budget.  No context, no cudaMalloc, no allocating library
  * call.  It has no counterpart in the reference.  Its scratch is a
- * fixed-size array of the library, 12.85 MB (3 * 2^20 + 2^16 + 256 32-bit
- * words), held by every CUDA context that uses it until the context ends,
+ * fixed-size array of the library, 13.11 MB (3 * 2^20 + 2^17 + 1,056
+ * 32-bit words), held by every CUDA context that uses it until the context
+ * ends,
  * so n is limited to AQUA_NOALLOC_SORT_MAX_KEYS; larger n returns
  * AQUA_ERR_CAPACITY.  keys are sorted in place (values below 2^key_bits),
  * perm[s] = original index and inv_perm[orig] = s (either may be NULL).
