@@ -820,6 +820,136 @@ class Trainer:
         return v
 
 
+class PairRing:
+    """A fixed-capacity ring of plain-step snapshot pairs on the device.
+    Each entry is (s0, s1, dt, offsets, cid): the states k steps apart, the
+    per-case time steps at s0, and the layout of the batch the pair came
+    from (case offsets, case of each particle).  A push past the capacity
+    overwrites the oldest entry."""
+
+    def __init__(self, capacity):
+        if capacity < 1:
+            raise ValueError("ring capacity must be >= 1")
+        self.capacity = int(capacity)
+        self.items = []
+        self.next = 0
+        self.pushed = 0
+
+    def __len__(self):
+        return len(self.items)
+
+    def push(self, item):
+        if len(self.items) < self.capacity:
+            self.items.append(item)
+        else:
+            self.items[self.next] = item
+        self.next = (self.next + 1) % self.capacity
+        self.pushed += 1
+
+    def sample(self, rng):
+        return self.items[int(rng.integers(len(self.items)))]
+
+
+def online_train(model, k, make_batch, n_runs=256, runs_per_gen=64,
+                 capacity=16, warm=20000, gap=300, pairs_per_gen=8,
+                 iters_per_pair=10, fit_pairs=4, cases_per_step=16, lr=1e-3,
+                 seed=0, fast=True, stream=None):
+    """Online training over many plain-solver runs.
+
+    Generations of ``runs_per_gen`` tanks (``make_batch(n_cases, g)`` gives
+    generation g's batch; n_runs / runs_per_gen generations) are stepped by
+    the plain solver.  After ``warm`` steps each generation emits
+    ``pairs_per_gen`` snapshot pairs k steps apart, ``gap`` steps apart,
+    into a PairRing of ``capacity`` pairs.  After each emission the trainer
+    takes ``iters_per_pair`` Adam steps, each on a pair drawn from the ring
+    and ``cases_per_step`` consecutive tanks of it.  The feature and target
+    scales are fitted on generation 0's first ``fit_pairs`` pairs before
+    the first step.  Returns the statistics of the run."""
+    from .solver import Solver
+    torch = _torch()
+    rng = np.random.default_rng(seed)
+    ring = PairRing(capacity)
+    gens = max(1, int(n_runs) // int(runs_per_gen))
+    tr = None
+    sv_graph = None
+    graph_cap = 0
+    iters = 0
+    losses = []
+    t_gen = t_train = 0.0
+    for gi in range(gens):
+        t0 = time.perf_counter()
+        batch = make_batch(runs_per_gen, gi)
+        c = batch.case
+        sv = Solver(c.params, capacity=c.N,
+                    ihoc_capacity=batch.n_cases * c.params.max_cells())
+        sv.set_precision(fast)
+        sv.set_batch(batch)
+        if warm:
+            sv.step(warm, graph=True, stream=stream)
+        offsets = np.asarray(batch.offsets, np.int64)
+        cid = case_ids(batch)
+        pending = []
+        for pi in range(pairs_per_gen):
+            s0 = Snapshot.capture(sv, c.dims, stream)
+            dt = torch.tensor([x["dt"] for x in sv.case_scalars(stream)],
+                              dtype=torch.float32, device="cuda")
+            sv.step(k, graph=True, stream=stream)
+            s1 = Snapshot.capture(sv, c.dims, stream)
+            item = (s0, s1, dt, offsets, cid)
+            ring.push(item)
+            if gap and pi + 1 < pairs_per_gen:
+                sv.step(gap, graph=True, stream=stream)
+            if tr is None:
+                # the scales from generation 0's first pairs, then training
+                pending.append(item)
+                if len(pending) < min(fit_pairs, pairs_per_gen):
+                    continue
+                fit_scales(model, [(a, b) for a, b, _, _, _ in pending],
+                           [d for _, _, d, _, _ in pending], k, c.params, cid)
+                # the graph context (grown when a slice does not fit)
+                graph_cap = c.N
+                sv_graph = Solver(c.params, capacity=graph_cap)
+                tr = Trainer(model, sv_graph, batch, k, lr=lr,
+                             cases_per_step=cases_per_step, seed=seed)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            t_gen += t1 - t0
+            for _ in range(iters_per_pair):
+                s0_, s1_, dt_, off_, cid_ = ring.sample(rng)
+                tr.offsets, tr.cid = off_, cid_
+                nc = len(off_) - 1
+                a = int(rng.integers(0, max(nc - cases_per_step, 0) + 1))
+                b = min(a + cases_per_step, nc)
+                n_slice = int(off_[b] - off_[a])
+                if n_slice > graph_cap:
+                    # a larger slice than any before: a larger graph context
+                    sv_graph.close()
+                    graph_cap = n_slice + n_slice // 4
+                    sv_graph = Solver(c.params, capacity=graph_cap)
+                    tr.sv = sv_graph
+                net, loss, dout, _ = tr.batch_loss((s0_, s1_), dt_, a, b)
+                model.grad.zero_()
+                net.backward(dout)
+                model.adam(lr)
+                losses.append(float(loss.item()))
+                iters += 1
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            t_train += t0 - t1
+        sv.check(stream)
+        sv.close()
+        t_gen += time.perf_counter() - t0
+    if sv_graph is not None:
+        sv_graph.close()
+    return {"runs": gens * int(runs_per_gen), "generations": gens,
+            "runs_per_generation": int(runs_per_gen), "ring_capacity": capacity,
+            "pairs_pushed": ring.pushed, "iterations": iters,
+            "warm_steps": warm, "gap_steps": gap, "cases_per_step": cases_per_step,
+            "loss_first": losses[0] if losses else None,
+            "loss_last10": float(np.mean(losses[-10:])) if losses else None,
+            "generate_s": t_gen, "train_s": t_train}
+
+
 # ---------------------------------------------------------------- proposal ----
 
 class ProposalRunner:

@@ -606,6 +606,7 @@ def learned_summary(args):
     and the held-out gain of the trained network over extrapolation."""
     la = argparse.Namespace(**vars(args))
     la.train_pairs, la.train_iters = args.learned_pairs, args.learned_iters
+    la.train_runs = args.learned_runs
     # trained on and evaluated in the same regime: after learned_warm plain
     # steps the sloshing has reached the left-wall probes
     la.steps, la.warmup, la.eval_warm = 5, 3, args.learned_warm
@@ -631,7 +632,9 @@ def learned_summary(args):
 def learned_c3(args):
     """Learned k = 8 proposals with a plain judge on a quarter of the cases,
     on the 64-tank sloshing batch; the network is first trained on plain
-    trajectories of 32 other tanks drawn from the same distribution.
+    trajectories of other tanks drawn from the same distribution: online
+    over ``train_runs`` runs (generations of 64 tanks through a ring of
+    snapshot pairs), or, with train_runs = 0, on one 32-tank trajectory.
     Returns the bench line."""
     import torch
     from aquagpusph_gb300 import case as cases
@@ -640,14 +643,35 @@ def learned_c3(args):
     torch.cuda.set_device(0)
     K = 8
     t0 = time.perf_counter()
-    tb = cases.sloshing_batch_2d(n_cases=32, seed=1234)
-    pairs, dts = Lm.collect_pairs(tb, K, n_pairs=args.train_pairs, gap=300,
-                                  warm=getattr(args, "train_warm", 500))
+    train_warm = getattr(args, "train_warm", 500)
+    runs = getattr(args, "train_runs", 0)
     model = Lm.Model(2, seed=0)
-    Lm.fit_scales(model, pairs, dts, K, tb.case.params, Lm.case_ids(tb))
+    if runs:
+        # online: generations of 64 tanks (seeds 1234, 1235, ...) through a
+        # ring of snapshot pairs; held out: 16 tanks of seed 999
+        per_pair = max(1, -(-args.train_iters // (max(1, runs // 64) * 8)))
+        online = Lm.online_train(
+            model, K, lambda n, g: cases.sloshing_batch_2d(n_cases=n, seed=1234 + g),
+            n_runs=runs, runs_per_gen=64, capacity=16, warm=train_warm, gap=300,
+            pairs_per_gen=8, iters_per_pair=per_pair, cases_per_step=16,
+            lr=1e-3, seed=0)
+        tb = cases.sloshing_batch_2d(n_cases=16, seed=999)
+        pairs, dts = Lm.collect_pairs(tb, K, n_pairs=4, gap=300, warm=train_warm)
+        held = list(range(len(pairs)))
+        train_desc = {"tanks": f"{online['runs']} sloshing runs of the config-2 "
+                               "distribution in generations of 64 (seeds 1234 + "
+                               "generation), online through a ring of snapshot "
+                               "pairs; held out: 16 tanks, seed 999",
+                      **online}
+        train_s = online["train_s"]
+    else:
+        tb = cases.sloshing_batch_2d(n_cases=32, seed=1234)
+        pairs, dts = Lm.collect_pairs(tb, K, n_pairs=args.train_pairs, gap=300,
+                                      warm=train_warm)
+        Lm.fit_scales(model, pairs, dts, K, tb.case.params, Lm.case_ids(tb))
+        held = list(range(len(pairs) - 4, len(pairs)))
     sv_t = Solver(tb.case.params, capacity=tb.case.N)
     tr = Lm.Trainer(model, sv_t, tb, K, lr=1e-3, cases_per_step=16)
-    held = list(range(len(pairs) - 4, len(pairs)))
 
     def held_loss(m):
         tr.model = m
@@ -661,12 +685,16 @@ def learned_c3(args):
     zero.scales.copy_(model.scales)
     zero.out_scale = model.out_scale
     loss_zero = held_loss(zero)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    for _ in range(args.train_iters):
-        tr.step(pairs[:-4], dts[:-4])
-    torch.cuda.synchronize()
-    train_s = time.perf_counter() - t1
+    if not runs:
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(args.train_iters):
+            tr.step(pairs[:-4], dts[:-4])
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t1
+        train_desc = {"tanks": "32 sloshing tanks, seed 1234 (config-2 distribution)",
+                      "pairs": args.train_pairs, "iterations": args.train_iters,
+                      "first_pair_after_steps": train_warm, "cases_per_step": 16}
     loss_trained = held_loss(model)
     sv_t.close()
     prep_s = time.perf_counter() - t0
@@ -766,11 +794,7 @@ def learned_c3(args):
         "config": {"workload": workload_desc("c3") if K == 8 else
                    workload_desc("c2") + f"; one step = one proposal of k={K} "
                    "plain steps", "training": {
-                       "tanks": "32 sloshing tanks, seed 1234 (config-2 distribution)",
-                       "pairs": args.train_pairs, "iterations": args.train_iters,
-                       "first_pair_after_steps": getattr(args, "train_warm", 500),
-                       "cases_per_step": 16, "train_s": train_s,
-                       "prep_s": prep_s},
+                       **train_desc, "train_s": train_s, "prep_s": prep_s},
                    "judge": "plain step re-run of 25% of the cases; rollback at "
                             "> 2% probe-pressure error (of max(|p|, rho g 4h)) "
                             "or > 2% density error (of refd)"},
@@ -1055,6 +1079,12 @@ def main():
     ap.add_argument("--no-learned", action="store_true",
                     help="c1: leave out the learned-proposal sub-object")
     ap.add_argument("--learned-pairs", type=int, default=24)
+    ap.add_argument("--learned-runs", type=int, default=256,
+                    help="runs of the online trainer of the learned sub-object "
+                         "(0: one 32-tank trajectory of --learned-pairs pairs)")
+    ap.add_argument("--train-runs", type=int, default=256,
+                    help="runs of the online trainer of --workload c3 (0: one "
+                         "32-tank trajectory of --train-pairs pairs)")
     ap.add_argument("--learned-iters", type=int, default=300)
     ap.add_argument("--learned-warm", type=int, default=20000)
     ap.add_argument("--train-warm", type=int, default=500,

@@ -186,6 +186,23 @@ def test_training_reduces_the_loss(torch):
     sv.close()
 
 
+def test_online_training_over_generations(torch):
+    """The online trainer steps three generations of two tanks each through
+    a ring of three snapshot pairs (more pairs than it holds), takes the
+    configured Adam steps and lowers the loss."""
+    from aquagpusph_gb300 import learned as Lm
+    k = 8
+    model = Lm.Model(2, seed=1)
+    st = Lm.online_train(model, k, lambda n, g: small_batch(n, seed=20 + g),
+                         n_runs=6, runs_per_gen=2, capacity=3, warm=100, gap=20,
+                         pairs_per_gen=2, iters_per_pair=15, fit_pairs=2,
+                         cases_per_step=2, lr=2e-3, seed=0)
+    assert st["runs"] == 6 and st["generations"] == 3
+    assert st["pairs_pushed"] == 6 and st["iterations"] == 3 * 2 * 15 - 15
+    assert np.isfinite(st["loss_last10"])
+    assert st["loss_last10"] < st["loss_first"], st
+
+
 def test_proposal_judge_and_rollback(torch):
     from aquagpusph_gb300 import learned as Lm
     from aquagpusph_gb300.solver import Solver
