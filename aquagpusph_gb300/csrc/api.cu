@@ -248,6 +248,7 @@ layout(aqua_ctx* x, char* base)
     b.cell_mark = cv.take<uint8_t>(x->ncap);
     b.work = cv.take<uint2>(n);
     b.wcl = cv.take<uint4>(n);
+    b.crow = cv.take<uint2>((size_t)9 * x->ncap);
     b.clu = cv.take<uint2>(n);
     b.cperm = cv.take<uint32_t>(n);
     x->sc = cv.take<DevScalars>(1);

@@ -176,14 +176,17 @@ struct StepBufs
     // (boundary element, its area) or 0 (no neighbour sums), rec1 = (u, p)
     // (fluid) or (normal, u.normal) (boundary element); the cells holding
     // particles as (key, first sorted index) in `work`, their cluster
-    // ranges in `wcl` (first, end, first cluster, clusters); clusters of
-    // <= 8 particles of one cell octant as (first position in cperm,
-    // count); cperm = sorted indices in cluster order
+    // ranges in `wcl` (first, end, case, clusters; the cell's clusters
+    // start at index `first` of `clu`), the (first sorted index, count) of
+    // the 9 rows of 3 cells around each in `crow`; clusters of <= 8
+    // particles of one cell octant as (first position in cperm, count);
+    // cperm = sorted indices in cluster order
     float4* rec0;
     float4* rec1;
     uint8_t* cell_mark;    // rate sample: cells around a probe (ncap)
     uint2* work;
     uint4* wcl;
+    uint2* crow;           // 9 per listed cell (ncap cells at most)
     uint2* clu;
     uint32_t* cperm;
 };

@@ -22,7 +22,7 @@ launch_cl(const Consts& c, const StepArgs& a, unsigned grid, unsigned sms,
 {
     constexpr uint32_t kPer = kCellListThreads * kCellListItems;
     k_cell_list<<<max(1u, (a.N + kPer - 1) / kPer), kCellListThreads, 0, s>>>(
-        a.skeys, a.N, a.b.work, a.sc);
+        a.skeys, a.N, a.b.cells, a.dst.cid, a.b.work, a.b.wcl, a.sc);
     k_clusters<<<sms * 8u, 256, 0, s>>>(c, a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)

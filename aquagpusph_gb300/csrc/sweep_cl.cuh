@@ -75,15 +75,17 @@ struct ClSmem
     uint64_t mbar;
 };
 
-// The cells holding particles, as (key, first sorted index): position s
-// starts a cell where the sorted key changes.  A block takes
+// The cells holding particles, as (key, first sorted index), and their
+// (first, end, -, case) in the cluster table: position s starts a cell
+// where the sorted key changes.  A block takes
 // kCellListThreads x kCellListItems positions and reserves its entries with
 // one atomicAdd (the order of the list does not matter: every cell is swept
 // the same wherever it sits in it).
 constexpr int kCellListThreads = 1024;
 constexpr int kCellListItems = 8;
 __global__ void __launch_bounds__(kCellListThreads)
-k_cell_list(const uint32_t* skeys, uint32_t N, uint2* work, DevScalars* sc)
+k_cell_list(const uint32_t* skeys, uint32_t N, const uint2* cells,
+            const uint32_t* cid, uint2* work, uint4* wcl, DevScalars* sc)
 {
     __shared__ uint32_t s_warp[kCellListThreads / 32];
     __shared__ uint32_t s_base;
@@ -124,7 +126,11 @@ k_cell_list(const uint32_t* skeys, uint32_t N, uint2* work, DevScalars* sc)
     for (int it = 0; it < kCellListItems; it++) {
         if (starts & (1u << it)) {
             const uint32_t s = base + it * kCellListThreads + threadIdx.x;
-            work[o++] = make_uint2(skeys[s], s);
+            const uint32_t key = skeys[s];
+            work[o] = make_uint2(key, s);
+            // (first, end, -, case) for k_clusters, which completes it
+            wcl[o] = make_uint4(s, cells[key].y, 0u, cid[s]);
+            o++;
         }
     }
 }
@@ -146,11 +152,29 @@ k_clusters(Consts c, StepArgs a)
     const uint32_t n_work = a.sc->n_chunks;
     const uint32_t lt = (1u << lane) - 1u;
     for (uint32_t w = blockIdx.x * 8u + warp; w < n_work; w += gridDim.x * 8u) {
-        const uint2 wk = a.b.work[w];
-        const uint32_t first = wk.y;
-        const uint32_t end = a.b.cells[wk.x].y;
+        const uint4 wc0 = a.b.wcl[w];  // (first, end, -, case) of k_cell_list
+        const uint32_t first = wc0.x;
+        const uint32_t end = wc0.y;
         const uint32_t n = end - first;
-        const CaseScalars& cs = a.cs[a.dst.cid[first]];
+        const CaseScalars& cs = a.cs[wc0.w];
+        if (lane < 9) {
+            // row (dy, dz) = (lane % 3 - 1, lane / 3 - 1) of the sweep's
+            // neighbourhood: cells x-1 .. x+1, as one run of sorted indices
+            const uint32_t key = a.b.work[w].x;
+            const uint32_t nx = cs.n_cells[0];
+            const uint32_t nxy = cs.n_cells[0] * cs.n_cells[1];
+            const uint32_t k0 = key + (uint32_t)(lane % 3 - 1) * nx +
+                                (uint32_t)(lane / 3 - 1) * nxy - 1u;
+            uint32_t lo = 0xffffffffu, hi = 0;
+            for (int d = 0; d < 3; d++) {
+                const uint2 se = a.b.cells[k0 + d];
+                if (se.x < se.y) {
+                    lo = min(lo, se.x);
+                    hi = max(hi, se.y);
+                }
+            }
+            a.b.crow[(size_t)w * 9 + lane] = hi > lo ? make_uint2(lo, hi - lo) : make_uint2(0u, 0u);
+        }
         const float sc2 = 2.f * c.idist;
         auto group = [&](uint32_t s) -> uint32_t {
             if (a.dst.imove[s] == 0)
@@ -213,8 +237,10 @@ k_clusters(Consts c, StepArgs a)
                 }
                 return k;
             };
+            // a cell has at most as many clusters as particles: its
+            // clusters take the slots of clu from its first sorted index on
             const uint32_t n_cl = walk(true, first) - first;
-            a.b.wcl[w] = make_uint4(first, end, first, n_cl);
+            a.b.wcl[w] = make_uint4(first, end, wc0.w, n_cl);
         }
         __syncwarp();
         if (lane < 16)
@@ -598,46 +624,38 @@ k_sweep_cl(Consts c, StepArgs a)
     };
 
     const uint32_t n_work = a.sc->n_chunks;
-    for (;;) {
-        // one thread decides for the block (another block may set the error
-        // word at any time: every thread must see the same decision)
-        if (tid == 0) {
-            uint32_t w = a.sc->err ? 0xffffffffu : atomicAdd(&a.sc->chunk_next, 1u);
-            // rate sample: skip the cells outside it
-            while (c.sample_on && w < n_work) {
-                const uint32_t k = a.b.work[w].x;
-                if (sample_hash(k, c.sample_seed) < c.sample_thr || a.b.cell_mark[k])
-                    break;
-                w = atomicAdd(&a.sc->chunk_next, 1u);
-            }
-            S.work = w;
+    // The next cell of the block (one thread decides for the block: another
+    // block may set the error word at any time, and every thread must see
+    // the same decision).  Thread 0 takes the next cell's index while the
+    // current cell is swept; it reaches S.work before the cell's last
+    // barrier.
+    auto fetch = [&]() -> uint32_t {
+        uint32_t w = a.sc->err ? 0xffffffffu : atomicAdd(&a.sc->chunk_next, 1u);
+        // rate sample: skip the cells outside it
+        while (c.sample_on && w < n_work) {
+            const uint32_t k = a.b.work[w].x;
+            if (sample_hash(k, c.sample_seed) < c.sample_thr || a.b.cell_mark[k])
+                break;
+            w = atomicAdd(&a.sc->chunk_next, 1u);
         }
-        __syncthreads();
+        return w;
+    };
+    if (tid == 0)
+        S.work = fetch();
+    __syncthreads();
+    uint32_t w_next = 0xffffffffu;  // thread 0
+    for (;;) {
         const uint32_t w = S.work;
         if (w >= n_work)
             break;
         const uint4 wc = a.b.wcl[w];
         const uint32_t key = a.b.work[w].x;
         const uint32_t n_cl = wc.w;
-        const uint32_t kc = T.cid[wc.x];
+        const uint32_t kc = wc.z;
         const CaseScalars& cas = a.cs[kc];
         const float dt = cas.dt;
-        if (warp == 0 && lane < 9) {
-            // row (dy, dz) = (lane % 3 - 1, lane / 3 - 1): cells x-1 .. x+1
-            const uint32_t nx = cas.n_cells[0];
-            const uint32_t nxy = cas.n_cells[0] * cas.n_cells[1];
-            const uint32_t k0 = key + (uint32_t)(lane % 3 - 1) * nx +
-                                (uint32_t)(lane / 3 - 1) * nxy - 1u;
-            uint32_t lo = 0xffffffffu, hi = 0;
-            for (int d = 0; d < 3; d++) {
-                const uint2 se = a.b.cells[k0 + d];
-                if (se.x < se.y) {
-                    lo = min(lo, se.x);
-                    hi = max(hi, se.y);
-                }
-            }
-            S.row[lane] = hi > lo ? make_uint2(lo, hi - lo) : make_uint2(0u, 0u);
-        }
+        if (warp == 0 && lane < 9)
+            S.row[lane] = a.b.crow[(size_t)w * 9 + lane];
         __syncthreads();
         if (tid == 0) {
             uint32_t t = 0;
@@ -649,6 +667,8 @@ k_sweep_cl(Consts c, StepArgs a)
         const uint32_t npass = (S.total + CAP - 1) / CAP;
         const bool single = npass <= 1;
         bool failed = !stage(0);
+        if (tid == 0)
+            w_next = fetch();  // consumed at the end of this cell
         // single pass: each warp takes every NW-th cluster; several passes:
         // waves of NW clusters, each wave re-staging every pass
         const uint32_t waves = single ? 1u : (n_cl + NW - 1) / NW;
@@ -662,7 +682,7 @@ k_sweep_cl(Consts c, StepArgs a)
                 // ---- cluster set-up
                 uint2 cl = make_uint2(0u, 0u);
                 if (have)
-                    cl = a.b.clu[wc.z + ci];
+                    cl = a.b.clu[wc.x + ci];
                 const bool valid = (uint32_t)mq < cl.y;
                 const uint32_t i = a.b.cperm[cl.x + (valid ? (uint32_t)mq : 0u)];
                 const float4 r0i = a.b.rec0[i];
@@ -939,6 +959,8 @@ k_sweep_cl(Consts c, StepArgs a)
         }
         if (failed)
             break;
+        if (tid == 0)
+            S.work = w_next;  // every thread read this cell's S.work long ago
         __syncthreads();  // the staged records are rewritten for the next cell
     }
     flush();
