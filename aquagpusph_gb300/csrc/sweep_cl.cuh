@@ -49,7 +49,8 @@
 
 namespace {
 
-constexpr int kClListCap = 128;      // fluid survivors per warp (ring of quads)
+constexpr int kClRounds = 3;         // filter rounds of 32 candidates per iteration
+constexpr int kClListCap = 64 * kClRounds;  // fluid survivors per warp
 constexpr int kClWallCap = 192;      // boundary-element survivors per warp
 constexpr int kClMaxPieces = 32;     // staged runs per pass
 constexpr uint32_t kClWaitLimit = 1u << 22;
@@ -845,20 +846,24 @@ k_sweep_cl(Consts c, StepArgs a)
                         const float bz = fmaxf(fabsf(pc.z - bc[2]) - be[2], 0.f);
                         return (bx * bx + by * by + bz * bz < R2) && pc.w > 0.f;
                     };
-                    // two independent rounds of 32 candidates per iteration
-                    for (uint32_t base = 0; base < nst; base += 64) {
-                        const uint32_t s0 = base + lane, s1 = base + 32 + lane;
-                        const bool f0 = near_fluid(s0);
-                        const bool f1 = near_fluid(s1);
-                        const unsigned b0 = __ballot_sync(0xffffffffu, f0);
-                        const unsigned b1 = __ballot_sync(0xffffffffu, f1);
-                        const uint32_t c0 = (uint32_t)__popc(b0);
-                        if (f0)
-                            list[fill + __popc(b0 & lt)] = (uint16_t)s0;
-                        if (f1)
-                            list[fill + c0 + __popc(b1 & lt)] = (uint16_t)s1;
-                        fill += c0 + (uint32_t)__popc(b1);
-                        if (fill > (uint32_t)(kClListCap - 64)) {
+                    // kClRounds independent rounds of 32 candidates per
+                    // iteration (their loads in flight together)
+                    for (uint32_t base = 0; base < nst; base += 32 * kClRounds) {
+                        bool f[kClRounds];
+                        unsigned bl[kClRounds];
+#pragma unroll
+                        for (int r = 0; r < kClRounds; r++)
+                            f[r] = near_fluid(base + 32u * r + lane);
+#pragma unroll
+                        for (int r = 0; r < kClRounds; r++)
+                            bl[r] = __ballot_sync(0xffffffffu, f[r]);
+#pragma unroll
+                        for (int r = 0; r < kClRounds; r++) {
+                            if (f[r])
+                                list[fill + __popc(bl[r] & lt)] = (uint16_t)(base + 32u * r + lane);
+                            fill += (uint32_t)__popc(bl[r]);
+                        }
+                        if (fill > (uint32_t)(kClListCap - 32 * kClRounds)) {
                             __syncwarp();
                             const uint32_t nq = fill / 4;
                             drain(list, nq, false);
