@@ -762,21 +762,19 @@ k_sweep_cl(Consts c, StepArgs a)
                     dbi = dbi - nj.w * wa;
                 };
                 // sums the first nq quads of a list (lane takes slot q); the
-                // records of the next entry are loaded during this one's sums
+                // load latency is left to the other resident warps (a
+                // software prefetch of the next entry cost registers and
+                // was slower)
                 auto drain = [&](const uint16_t* lst, uint32_t nq, bool walls) {
                     if (nq == 0)
                         return;
-                    uint32_t j = lst[q];
-                    float4 a0 = S.r0[j], a1 = S.r1[j];
                     for (uint32_t t = 0; t < nq; t++) {
-                        const uint32_t jn = lst[4 * min(t + 1, nq - 1) + q];
-                        const float4 b0 = S.r0[jn], b1 = S.r1[jn];
+                        const uint32_t j = lst[4 * t + q];
+                        const float4 a0 = S.r0[j], a1 = S.r1[j];
                         if (walls)
                             wall_pair(a0, a1);
                         else
                             fluid_pair(a0, a1);
-                        a0 = b0;
-                        a1 = b1;
                     }
                 };
 
