@@ -18,13 +18,18 @@
 // particle l % 8 and takes every fourth neighbour of the cluster's list from
 // slot l / 8 on, so that the 8 lanes of one phase of a 16-byte shared load
 // read the same record (a broadcast, free of bank conflicts).
-// The list holds the staged candidates within the support of the
-// cluster's bounding box (a lane-parallel filter over the staged records,
-// compacted with ballots), so about 60% of the evaluated pairs lie in the
-// support on a lattice, against about a third of the lanes in k_sweep.
-// Pairs outside the support add exact zeros (the kernel factor is cut to
-// zero at q >= SUPPORT), so the filter only has to be conservative.  The
-// four partial sums of a particle are added by two butterfly shuffles.
+// The list holds the staged candidates within the support of the octant
+// boxes of the cluster's particles.  After each staging the block
+// classifies every staged record once: its kind (fluid, boundary element)
+// and the octant boxes of the cell it comes within the support of (a box
+// per octant, spanning, per axis and half, the cell's particles there).
+// Each cluster then scans those 16-bit masks and compacts its candidates
+// with ballots.  About 60% of the evaluated pairs lie in the support on a
+// lattice, against about a third of the lanes in k_sweep.  Pairs outside
+// the support add exact zeros (the kernel factor is cut to zero at
+// q >= SUPPORT), so the lists only have to be conservative: each octant
+// box holds its particles.  The four partial sums of a particle are added
+// by two butterfly shuffles.
 //
 // Summation order differs from the reference's (neighbours in staging
 // order, four interleaved partial sums): this sweep is the fast build's,
@@ -52,6 +57,10 @@ namespace {
 constexpr int kClRounds = 3;         // filter rounds of 32 candidates per iteration
 constexpr int kClListCap = 64 * kClRounds;  // fluid survivors per warp
 constexpr int kClWallCap = 192;      // boundary-element survivors per warp
+// per staged record: bit o (o < 8) = within the support of the cell's
+// octant box o; the record's kind
+constexpr uint32_t kMaskFluid = 1u << 8;
+constexpr uint32_t kMaskWall = 1u << 9;
 constexpr int kClMaxPieces = 32;     // staged runs per pass
 constexpr uint32_t kClWaitLimit = 1u << 22;
 
@@ -65,8 +74,8 @@ struct ClSmem
     uint16_t list[NW][kClListCap + 4];   // + room for the padding quad
     uint16_t wall[NW][kClWallCap + 4];
     // the staged boundary elements, by warp-sized chunks of the staging
-    uint16_t wsub[NW][((CAP + NW * 32 - 1) / (NW * 32)) * 32];
-    uint32_t wcnt[NW];
+    alignas(4) uint16_t mask[CAP + 2];  // per staged record (kMaskFluid, kMaskWall, octants)
+    float ivl[12];               // octant boxes: axis a, half h: [lo, hi] at 4 a + 2 h
     uint4 piece[kClMaxPieces];   // (slot, sorted first, count, -)
     uint2 row[9];                // (sorted first, count) of each row
     uint32_t npieces;
@@ -75,6 +84,17 @@ struct ClSmem
     uint32_t work;
     uint64_t mbar;
 };
+
+// Octant (0-7, x fastest) of a position inside its cell: the halves of the
+// cell along each axis (cells are (support h) wide from the case's r_min)
+__device__ __forceinline__ uint32_t
+cl_octant(const float4 p, const CaseScalars& cs, float sc2)
+{
+    const uint32_t ox = (uint32_t)((p.x - cs.r_min[0]) * sc2) & 1u;
+    const uint32_t oy = (uint32_t)((p.y - cs.r_min[1]) * sc2) & 1u;
+    const uint32_t oz = (uint32_t)((p.z - cs.r_min[2]) * sc2) & 1u;
+    return ox | (oy << 1) | (oz << 2);
+}
 
 // The cells holding particles, as (key, first sorted index), and their
 // (first, end, -, case) in the cluster table: position s starts a cell
@@ -180,11 +200,7 @@ k_clusters(Consts c, StepArgs a)
         auto group = [&](uint32_t s) -> uint32_t {
             if (a.dst.imove[s] == 0)
                 return 8u;
-            const float4 p = a.b.rec0[s];
-            const uint32_t ox = (uint32_t)((p.x - cs.r_min[0]) * sc2) & 1u;
-            const uint32_t oy = (uint32_t)((p.y - cs.r_min[1]) * sc2) & 1u;
-            const uint32_t oz = (uint32_t)((p.z - cs.r_min[2]) * sc2) & 1u;
-            return ox | (oy << 1) | (oz << 2);
+            return cl_octant(a.b.rec0[s], cs, sc2);
         };
         if (lane < 16)
             s_cnt[warp][lane] = 0;
@@ -590,25 +606,41 @@ k_sweep_cl(Consts c, StepArgs a)
                 atomicOr(&a.sc->err, kErrTimeout);
             return false;
         }
-        // the boundary elements among the staged records (few): warp w
-        // lists those of its chunk, in staging order
+        // classify the staged records once for all the cell's clusters:
+        // their kind, and which octant boxes of the cell (S.ivl) they come
+        // within the support of (box distance per axis and half, summed
+        // over the 8 combinations)
         {
             const uint32_t nst = S.nstaged;
-            constexpr uint32_t kChunk = ((CAP + NW * 32 - 1) / (NW * 32)) * 32;
-            const uint32_t chunk = ((nst + NW * 32 - 1) / (NW * 32)) * 32;
-            const uint32_t lo = (uint32_t)warp * chunk;
-            const uint32_t hi = min(nst, lo + chunk);
-            uint32_t cnt = 0;
-            for (uint32_t b = lo; b < hi; b += 32) {
-                const uint32_t k = b + lane;
-                const bool w = k < hi && S.r0[k].w < 0.f;
-                const unsigned bal = __ballot_sync(0xffffffffu, w);
-                if (w && cnt + __popc(bal & lt) < kChunk)
-                    S.wsub[warp][cnt + __popc(bal & lt)] = (uint16_t)k;
-                cnt += (uint32_t)__popc(bal);
+            float lo[6], hi[6];
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                lo[q] = S.ivl[2 * q];
+                hi[q] = S.ivl[2 * q + 1];
             }
-            if (lane == 0)
-                S.wcnt[warp] = cnt;
+            for (uint32_t k = tid; k < nst; k += NW * 32) {
+                const float4 pc = S.r0[k];
+                uint32_t m = pc.w > 0.f ? kMaskFluid : (pc.w < 0.f ? kMaskWall : 0u);
+                if (m) {
+                    const float x[3] = { pc.x, pc.y, pc.z };
+                    float d2[6];
+#pragma unroll
+                    for (int q = 0; q < 6; q++) {
+                        const float d = fmaxf(fmaxf(lo[q] - x[q >> 1], x[q >> 1] - hi[q]), 0.f);
+                        d2[q] = d * d;
+                    }
+                    // (x half, y half) combinations, then z
+                    const float dxy[4] = { d2[0] + d2[2], d2[1] + d2[2],
+                                           d2[0] + d2[3], d2[1] + d2[3] };
+#pragma unroll
+                    for (int o = 0; o < 8; o++)
+                        if (dxy[o & 3] + d2[4 + (o >> 2)] < R2)
+                            m |= 1u << o;
+                }
+                S.mask[k] = (uint16_t)m;
+            }
+            if (tid == 0)
+                S.mask[nst] = 0;  // read as the pair of an odd last record
         }
         __syncthreads();
         return true;
@@ -667,6 +699,54 @@ k_sweep_cl(Consts c, StepArgs a)
         __syncthreads();
         const uint32_t npass = (S.total + CAP - 1) / CAP;
         const bool single = npass <= 1;
+        if (warp == NW - 1) {
+            // the octant boxes of the cell: per axis and half, the extent of
+            // the cell's particles that take neighbour sums (probes apart);
+            // an empty half stays [+inf, -inf] and is never within reach.
+            // Ready before the classification (stage's barrier).
+            const float sc2 = 2.f * c.idist;
+            float bl[6], bh[6];
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                bl[q] = INFINITY;
+                bh[q] = -INFINITY;
+            }
+            for (uint32_t sidx = wc.x + lane; sidx < wc.y; sidx += 32) {
+                const int imv = T.imove[sidx];
+                if (imv < -3 || imv > 1 || imv == 0)
+                    continue;
+                const float4 p = a.b.rec0[sidx];
+                const uint32_t o = cl_octant(p, cas, sc2);
+                const float x[3] = { p.x, p.y, p.z };
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) {
+                    // constant indices (registers): half 0 or 1 by select
+                    const bool up = (o >> ax) & 1u;
+                    bl[2 * ax] = up ? bl[2 * ax] : fminf(bl[2 * ax], x[ax]);
+                    bh[2 * ax] = up ? bh[2 * ax] : fmaxf(bh[2 * ax], x[ax]);
+                    bl[2 * ax + 1] = up ? fminf(bl[2 * ax + 1], x[ax]) : bl[2 * ax + 1];
+                    bh[2 * ax + 1] = up ? fmaxf(bh[2 * ax + 1], x[ax]) : bh[2 * ax + 1];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    bl[q] = fminf(bl[q], __shfl_xor_sync(0xffffffffu, bl[q], o));
+                    bh[q] = fmaxf(bh[q], __shfl_xor_sync(0xffffffffu, bh[q], o));
+                }
+            }
+            if (lane < 6) {
+                float l = bl[0], h = bh[0];
+#pragma unroll
+                for (int q = 1; q < 6; q++)
+                    if (lane == (uint32_t)q) {
+                        l = bl[q];
+                        h = bh[q];
+                    }
+                S.ivl[2 * lane] = l;
+                S.ivl[2 * lane + 1] = h;
+            }
+        }
         bool failed = !stage(0);
         if (tid == 0)
             w_next = fetch();  // consumed at the end of this cell
@@ -694,26 +774,13 @@ k_sweep_cl(Consts c, StepArgs a)
                 const bool sensor = valid && im == 0;
                 const bool any_fluid = __any_sync(0xffffffffu, fluid);
                 const bool probes = __any_sync(0xffffffffu, sensor);
-                float blo[3], bhi[3];
-                {
-                    const float ri[3] = { r0i.x, r0i.y, r0i.z };
-                    for (int d = 0; d < 3; d++) {
-                        float lo = want ? ri[d] : INFINITY;
-                        float hi = want ? ri[d] : -INFINITY;
-                        for (int o = 16; o > 0; o >>= 1) {
-                            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-                            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-                        }
-                        blo[d] = lo;
-                        bhi[d] = hi;
-                    }
-                }
-                const bool any_want = blo[0] <= bhi[0];
-                float bc[3], be[3];  // box centre and half-extent
-                for (int d = 0; d < 3; d++) {
-                    bc[d] = 0.5f * (blo[d] + bhi[d]);
-                    be[d] = 0.5f * (bhi[d] - blo[d]);
-                }
+                const bool any_want = __any_sync(0xffffffffu, want);
+                // the octants of the cluster's particles that take sums: the
+                // candidates are the staged records within the support of
+                // any of those octant boxes (each box holds its particles,
+                // so the list is conservative)
+                const uint32_t omask = __reduce_or_sync(
+                    0xffffffffu, want && !sensor ? 1u << cl_octant(r0i, cas, 2.f * c.idist) : 0u);
                 float shep = 0.f, gp0 = 0.f, gp1 = 0.f, gp2 = 0.f;
                 float lu0 = 0.f, lu1 = 0.f, lu2 = 0.f, du = 0.f, lp = 0.f;
                 float gw0 = 0.f, gw1 = 0.f, gw2 = 0.f, dbi = 0.f;
@@ -835,66 +902,32 @@ k_sweep_cl(Consts c, StepArgs a)
                     }
                     uint32_t fill = 0;
                     uint32_t wdone = wfill;  // wall entries already summed
-                    auto near_fluid = [&](uint32_t s) -> bool {
-                        if (s >= nst)
-                            return false;
-                        const float4 pc = S.r0[s];
-                        const float bx = fmaxf(fabsf(pc.x - bc[0]) - be[0], 0.f);
-                        const float by = fmaxf(fabsf(pc.y - bc[1]) - be[1], 0.f);
-                        const float bz = fmaxf(fabsf(pc.z - bc[2]) - be[2], 0.f);
-                        return (bx * bx + by * by + bz * bz < R2) && pc.w > 0.f;
-                    };
-                    // kClRounds independent rounds of 32 candidates per
-                    // iteration (their loads in flight together)
-                    for (uint32_t base = 0; base < nst; base += 32 * kClRounds) {
-                        bool f[kClRounds];
-                        unsigned bl[kClRounds];
-#pragma unroll
-                        for (int r = 0; r < kClRounds; r++)
-                            f[r] = near_fluid(base + 32u * r + lane);
-#pragma unroll
-                        for (int r = 0; r < kClRounds; r++)
-                            bl[r] = __ballot_sync(0xffffffffu, f[r]);
-#pragma unroll
-                        for (int r = 0; r < kClRounds; r++) {
-                            if (f[r])
-                                list[fill + __popc(bl[r] & lt)] = (uint16_t)(base + 32u * r + lane);
-                            fill += (uint32_t)__popc(bl[r]);
-                        }
-                        if (fill > (uint32_t)(kClListCap - 32 * kClRounds)) {
-                            __syncwarp();
-                            const uint32_t nq = fill / 4;
-                            drain(list, nq, false);
-                            __syncwarp();
-                            const uint32_t rem = fill - 4 * nq;
-                            uint16_t mv = 0;
-                            if ((uint32_t)lane < rem)
-                                mv = list[4 * nq + lane];
-                            __syncwarp();
-                            if ((uint32_t)lane < rem)
-                                list[lane] = mv;
-                            fill = rem;
-                        }
-                    }
-                    // boundary elements (fluid clusters only): the staged
-                    // wall sub-lists in order
-                    for (int ws = 0; any_fluid && ws < NW; ws++) {
-                        const uint32_t wn = min(S.wcnt[ws], (uint32_t)(sizeof(S.wsub[0]) / 2));
-                        for (uint32_t b = 0; b < wn; b += 32) {
-                            bool wsv = false;
-                            uint32_t s = 0;
-                            if (b + lane < wn) {
-                                s = S.wsub[ws][b + lane];
-                                const float4 pc = S.r0[s];
-                                const float bx = fmaxf(fabsf(pc.x - bc[0]) - be[0], 0.f);
-                                const float by = fmaxf(fabsf(pc.y - bc[1]) - be[1], 0.f);
-                                const float bz = fmaxf(fabsf(pc.z - bc[2]) - be[2], 0.f);
-                                wsv = bx * bx + by * by + bz * bz < R2;
-                            }
-                            const unsigned bw = __ballot_sync(0xffffffffu, wsv);
-                            if (!bw)
-                                continue;
-                            if (wfill + (uint32_t)__popc(bw) > (uint32_t)kClWallCap) {
+                    const uint32_t wkind = any_fluid ? kMaskWall : 0u;
+                    // 64 records per round, two per lane (records 2l, 2l+1),
+                    // listed in staging order
+                    for (uint32_t base = 0; base < nst; base += 64) {
+                        const uint32_t k0 = base + 2u * lane;
+                        uint32_t mm = 0;
+                        if (k0 < nst)
+                            mm = *reinterpret_cast<const uint32_t*>(&S.mask[k0]);
+                        const uint32_t m0 = mm & 0xffffu, m1 = mm >> 16;
+                        const bool n0 = (m0 & omask) != 0u, n1 = (m1 & omask) != 0u;
+                        const bool f0 = n0 && (m0 & kMaskFluid), f1 = n1 && (m1 & kMaskFluid);
+                        const unsigned b0 = __ballot_sync(0xffffffffu, f0);
+                        const unsigned b1 = __ballot_sync(0xffffffffu, f1);
+                        const uint32_t p0 = fill + (uint32_t)(__popc(b0 & lt) + __popc(b1 & lt));
+                        if (f0)
+                            list[p0] = (uint16_t)k0;
+                        if (f1)
+                            list[p0 + (f0 ? 1u : 0u)] = (uint16_t)(k0 + 1u);
+                        fill += (uint32_t)(__popc(b0) + __popc(b1));
+                        // boundary elements (fluid clusters only)
+                        const bool w0 = n0 && (m0 & wkind), w1 = n1 && (m1 & wkind);
+                        const unsigned c0 = __ballot_sync(0xffffffffu, w0);
+                        const unsigned c1 = __ballot_sync(0xffffffffu, w1);
+                        if (c0 | c1) {
+                            const uint32_t nwall = (uint32_t)(__popc(c0) + __popc(c1));
+                            if (wfill + nwall > (uint32_t)kClWallCap) {
                                 // the wall list is full: sum it, and let the
                                 // epilogue walk the walls from global memory
                                 __syncwarp();
@@ -908,9 +941,26 @@ k_sweep_cl(Consts c, StepArgs a)
                                 wdone = 0;
                                 walls_global = true;
                             }
-                            if (wsv)
-                                wl[wfill + __popc(bw & lt)] = (uint16_t)s;
-                            wfill += (uint32_t)__popc(bw);
+                            const uint32_t q0 = wfill + (uint32_t)(__popc(c0 & lt) + __popc(c1 & lt));
+                            if (w0)
+                                wl[q0] = (uint16_t)k0;
+                            if (w1)
+                                wl[q0 + (w0 ? 1u : 0u)] = (uint16_t)(k0 + 1u);
+                            wfill += nwall;
+                        }
+                        if (fill > (uint32_t)(kClListCap - 64)) {
+                            __syncwarp();
+                            const uint32_t nq = fill / 4;
+                            drain(list, nq, false);
+                            __syncwarp();
+                            const uint32_t rem = fill - 4 * nq;
+                            uint16_t mv = 0;
+                            if ((uint32_t)lane < rem)
+                                mv = list[4 * nq + lane];
+                            __syncwarp();
+                            if ((uint32_t)lane < rem)
+                                list[lane] = mv;
+                            fill = rem;
                         }
                     }
                     // the rest of both lists, padded with the zero record
