@@ -74,7 +74,7 @@ struct ClSmem
     uint16_t list[NW][kClListCap + 4];   // + room for the padding quad
     uint16_t wall[NW][kClWallCap + 4];
     // the staged boundary elements, by warp-sized chunks of the staging
-    alignas(4) uint16_t mask[CAP + 2];  // per staged record (kMaskFluid, kMaskWall, octants)
+    alignas(8) uint16_t mask[CAP + 4];  // per staged record (kMaskFluid, kMaskWall, octants)
     float ivl[12];               // octant boxes: axis a, half h: [lo, hi] at 4 a + 2 h
     uint4 piece[kClMaxPieces];   // (slot, sorted first, count, -)
     uint2 row[9];                // (sorted first, count) of each row
@@ -639,8 +639,8 @@ k_sweep_cl(Consts c, StepArgs a)
                 }
                 S.mask[k] = (uint16_t)m;
             }
-            if (tid == 0)
-                S.mask[nst] = 0;  // read as the pair of an odd last record
+            if (tid < 3)
+                S.mask[nst + tid] = 0;  // read with the last records' group of 4
         }
         __syncthreads();
         return true;
@@ -903,31 +903,39 @@ k_sweep_cl(Consts c, StepArgs a)
                     uint32_t fill = 0;
                     uint32_t wdone = wfill;  // wall entries already summed
                     const uint32_t wkind = any_fluid ? kMaskWall : 0u;
-                    // 64 records per round, two per lane (records 2l, 2l+1),
-                    // listed in staging order
-                    for (uint32_t base = 0; base < nst; base += 64) {
-                        const uint32_t k0 = base + 2u * lane;
-                        uint32_t mm = 0;
+                    // 128 records per round, four per lane (records 4l ..
+                    // 4l+3), listed in staging order
+                    for (uint32_t base = 0; base < nst; base += 128) {
+                        const uint32_t k0 = base + 4u * lane;
+                        uint2 mm = make_uint2(0u, 0u);
                         if (k0 < nst)
-                            mm = *reinterpret_cast<const uint32_t*>(&S.mask[k0]);
-                        const uint32_t m0 = mm & 0xffffu, m1 = mm >> 16;
-                        const bool n0 = (m0 & omask) != 0u, n1 = (m1 & omask) != 0u;
-                        const bool f0 = n0 && (m0 & kMaskFluid), f1 = n1 && (m1 & kMaskFluid);
-                        const unsigned b0 = __ballot_sync(0xffffffffu, f0);
-                        const unsigned b1 = __ballot_sync(0xffffffffu, f1);
-                        const uint32_t p0 = fill + (uint32_t)(__popc(b0 & lt) + __popc(b1 & lt));
-                        if (f0)
-                            list[p0] = (uint16_t)k0;
-                        if (f1)
-                            list[p0 + (f0 ? 1u : 0u)] = (uint16_t)(k0 + 1u);
-                        fill += (uint32_t)(__popc(b0) + __popc(b1));
-                        // boundary elements (fluid clusters only)
-                        const bool w0 = n0 && (m0 & wkind), w1 = n1 && (m1 & wkind);
-                        const unsigned c0 = __ballot_sync(0xffffffffu, w0);
-                        const unsigned c1 = __ballot_sync(0xffffffffu, w1);
-                        if (c0 | c1) {
-                            const uint32_t nwall = (uint32_t)(__popc(c0) + __popc(c1));
-                            if (wfill + nwall > (uint32_t)kClWallCap) {
+                            mm = *reinterpret_cast<const uint2*>(&S.mask[k0]);
+                        const uint32_t m[4] = { mm.x & 0xffffu, mm.x >> 16, mm.y & 0xffffu, mm.y >> 16 };
+                        bool fl[4], wa[4];
+                        unsigned bf[4], bw[4];
+                        uint32_t before = 0, wbefore = 0, tot = 0, wtot = 0;
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const bool nu = (m[u] & omask) != 0u;
+                            fl[u] = nu && (m[u] & kMaskFluid);
+                            wa[u] = nu && (m[u] & wkind);
+                            bf[u] = __ballot_sync(0xffffffffu, fl[u]);
+                            bw[u] = __ballot_sync(0xffffffffu, wa[u]);
+                            before += (uint32_t)__popc(bf[u] & lt);
+                            wbefore += (uint32_t)__popc(bw[u] & lt);
+                            tot += (uint32_t)__popc(bf[u]);
+                            wtot += (uint32_t)__popc(bw[u]);
+                        }
+                        {
+                            uint32_t p = fill + before;
+#pragma unroll
+                            for (int u = 0; u < 4; u++)
+                                if (fl[u])
+                                    list[p++] = (uint16_t)(k0 + u);
+                        }
+                        fill += tot;
+                        if (wtot) {
+                            if (wfill + wtot > (uint32_t)kClWallCap) {
                                 // the wall list is full: sum it, and let the
                                 // epilogue walk the walls from global memory
                                 __syncwarp();
@@ -941,14 +949,14 @@ k_sweep_cl(Consts c, StepArgs a)
                                 wdone = 0;
                                 walls_global = true;
                             }
-                            const uint32_t q0 = wfill + (uint32_t)(__popc(c0 & lt) + __popc(c1 & lt));
-                            if (w0)
-                                wl[q0] = (uint16_t)k0;
-                            if (w1)
-                                wl[q0 + (w0 ? 1u : 0u)] = (uint16_t)(k0 + 1u);
-                            wfill += nwall;
+                            uint32_t q = wfill + wbefore;
+#pragma unroll
+                            for (int u = 0; u < 4; u++)
+                                if (wa[u])
+                                    wl[q++] = (uint16_t)(k0 + u);
+                            wfill += wtot;
                         }
-                        if (fill > (uint32_t)(kClListCap - 64)) {
+                        if (fill > (uint32_t)(kClListCap - 128)) {
                             __syncwarp();
                             const uint32_t nq = fill / 4;
                             drain(list, nq, false);
