@@ -54,8 +54,8 @@
 
 namespace {
 
-constexpr int kClRounds = 3;         // filter rounds of 32 candidates per iteration
-constexpr int kClListCap = 64 * kClRounds;  // fluid survivors per warp
+constexpr int kClListCap = 192;      // fluid survivors per warp (128 per round
+                                     // of the mask scan, drained above 64)
 constexpr int kClWallCap = 192;      // boundary-element survivors per warp
 // per staged record: bit o (o < 8) = within the support of the cell's
 // octant box o; the record's kind
