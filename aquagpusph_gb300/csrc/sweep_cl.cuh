@@ -178,23 +178,19 @@ k_clusters(Consts c, StepArgs a)
         const uint32_t end = wc0.y;
         const uint32_t n = end - first;
         const CaseScalars& cs = a.cs[wc0.w];
+        // row (dy, dz) = (lane % 3 - 1, lane / 3 - 1) of the sweep's
+        // neighbourhood: cells x-1 .. x+1, as one run of sorted indices
+        // (lanes 0-8; the cell table is read here and the row written after
+        // the clusters, so the loads overlap the work below)
+        uint2 rc3[3] = { make_uint2(1u, 0u), make_uint2(1u, 0u), make_uint2(1u, 0u) };
         if (lane < 9) {
-            // row (dy, dz) = (lane % 3 - 1, lane / 3 - 1) of the sweep's
-            // neighbourhood: cells x-1 .. x+1, as one run of sorted indices
             const uint32_t key = a.b.work[w].x;
             const uint32_t nx = cs.n_cells[0];
             const uint32_t nxy = cs.n_cells[0] * cs.n_cells[1];
             const uint32_t k0 = key + (uint32_t)(lane % 3 - 1) * nx +
                                 (uint32_t)(lane / 3 - 1) * nxy - 1u;
-            uint32_t lo = 0xffffffffu, hi = 0;
-            for (int d = 0; d < 3; d++) {
-                const uint2 se = a.b.cells[k0 + d];
-                if (se.x < se.y) {
-                    lo = min(lo, se.x);
-                    hi = max(hi, se.y);
-                }
-            }
-            a.b.crow[(size_t)w * 9 + lane] = hi > lo ? make_uint2(lo, hi - lo) : make_uint2(0u, 0u);
+            for (int d = 0; d < 3; d++)
+                rc3[d] = a.b.cells[k0 + d];
         }
         const float sc2 = 2.f * c.idist;
         auto group = [&](uint32_t s) -> uint32_t {
@@ -275,6 +271,16 @@ k_clusters(Consts c, StepArgs a)
             if (v && lane == __ffs(m) - 1)
                 s_cnt[warp][g] += (uint32_t)__popc(m);
             __syncwarp();
+        }
+        if (lane < 9) {
+            uint32_t lo = 0xffffffffu, hi = 0;
+            for (int d = 0; d < 3; d++) {
+                if (rc3[d].x < rc3[d].y) {
+                    lo = min(lo, rc3[d].x);
+                    hi = max(hi, rc3[d].y);
+                }
+            }
+            a.b.crow[(size_t)w * 9 + lane] = hi > lo ? make_uint2(lo, hi - lo) : make_uint2(0u, 0u);
         }
     }
 }
