@@ -564,9 +564,12 @@ k_edge_features_rec(uint32_t E, const uint32_t* __restrict__ recv,
         f[k++] = wall ? 1.f : 0.f;
         for (int d = 0; d < D; d++)
             f[k++] = wall ? nj[d] : 0.f;
-        uint16_t* row = out + (size_t)e * AQUA_GNN_FEATURES;
-        for (int m = 0; m < AQUA_GNN_FEATURES; m += 2)
-            *reinterpret_cast<uint32_t*>(row + m) = pack_bf2(f[m], f[m + 1]);
+        // the 32-byte row as two 16-byte stores
+        uint4* row = reinterpret_cast<uint4*>(out + (size_t)e * AQUA_GNN_FEATURES);
+        row[0] = make_uint4(pack_bf2(f[0], f[1]), pack_bf2(f[2], f[3]),
+                            pack_bf2(f[4], f[5]), pack_bf2(f[6], f[7]));
+        row[1] = make_uint4(pack_bf2(f[8], f[9]), pack_bf2(f[10], f[11]),
+                            pack_bf2(f[12], f[13]), pack_bf2(f[14], f[15]));
     }
 }
 
@@ -1485,7 +1488,8 @@ aqua_gnn_edge_features_rec(uint32_t E, int32_t dims, const uint32_t* recv,
                            const float* scales, uint16_t* out, void* stream)
 {
     if ((dims != 2 && dims != 3) || !recv || !send || !rec || !scales ||
-        !out || (reinterpret_cast<uintptr_t>(rec) & 15))
+        !out || (reinterpret_cast<uintptr_t>(rec) & 15) ||
+        (reinterpret_cast<uintptr_t>(out) & 15))
         return AQUA_ERR_INVALID;
     if (E == 0)
         return AQUA_OK;

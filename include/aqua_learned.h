@@ -106,7 +106,8 @@ aqua_status aqua_gnn_edge_features(uint32_t n_edges, int32_t dims,
 /* The same edge features from packed node records: rec (16-byte aligned,
  * AQUA_GNN_RECORD_FLOATS(dims) floats per node) is written by
  * aqua_gnn_node_records from the node-ordered r, u, rho, imove, normal;
- * the features are bit-identical to aqua_gnn_edge_features'. */
+ * the features are bit-identical to aqua_gnn_edge_features'.  out is
+ * 16-byte aligned (32-byte rows, stored as two 16-byte halves). */
 #define AQUA_GNN_RECORD_FLOATS(dims) ((dims) == 3 ? 12 : 8)
 aqua_status aqua_gnn_node_records(uint32_t n, int32_t dims, const float* r,
                                   const float* u, const float* rho,
