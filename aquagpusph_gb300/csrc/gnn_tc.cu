@@ -671,6 +671,8 @@ static_assert(edge_ctas_per_sm<true>() * (edge_mlp_smem<144>() + 1024) <= 228 * 
               "pair-input CTAs per SM");
 static_assert(edge_ctas_per_sm<false>() * (edge_mlp_smem<16>() + 1024) <= 228 * 1024,
               "row-input CTAs per SM");
+static_assert(edge_ctas_per_sm<false>() * (edge_mlp_smem<80>() + 1024) <= 228 * 1024,
+              "80-wide row-input CTAs per SM");
 
 
 // ---------------------------------------------------------------------------
@@ -1011,6 +1013,8 @@ edge_mlp_configure(int& sms)
         const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
         if (cudaFuncSetAttribute(k_edge_mlp_tc<16, false, false>, a,
                                  (int)edge_mlp_smem<16>()) != cudaSuccess ||
+            cudaFuncSetAttribute(k_edge_mlp_tc<80, false, false>, a,
+                                 (int)edge_mlp_smem<80>()) != cudaSuccess ||
             cudaFuncSetAttribute(k_edge_mlp_tc<144, true, false>, a,
                                  (int)edge_mlp_smem<144>()) != cudaSuccess ||
             cudaFuncSetAttribute(k_edge_mlp_tc<16, false, true>, a,
@@ -1029,9 +1033,10 @@ a16(const void* p)
     return (reinterpret_cast<uintptr_t>(p) & 15) == 0;
 }
 
-// the arguments both fused forms share
+// the arguments both fused forms share; row inputs are 16 wide (edge
+// features), or 80 wide where `rows80` (the first node MLP, n1)
 bool
-edge_mlp_args_ok(uint32_t K1, const uint16_t* X, uint32_t ldx,
+edge_mlp_args_ok(uint32_t K1, bool rows80, const uint16_t* X, uint32_t ldx,
                  const uint32_t* recv, const uint32_t* send, const uint16_t* H,
                  uint32_t ldh, const uint16_t* Ef, const uint16_t* W1,
                  const float* b1, const uint16_t* W2, const float* b2,
@@ -1043,7 +1048,8 @@ edge_mlp_args_ok(uint32_t K1, const uint16_t* X, uint32_t ldx,
     if (X == nullptr)
         return K1 == 144 && recv && send && H && Ef && ldh >= 64 && ldh % 8 == 0 &&
                a16(H) && a16(Ef);
-    return K1 == AQUA_GNN_FEATURES && ldx >= K1 && ldx % 8 == 0 && a16(X);
+    return (K1 == AQUA_GNN_FEATURES || (rows80 && K1 == 80)) && ldx >= K1 &&
+           ldx % 8 == 0 && a16(X);
 }
 
 }  // namespace
@@ -1058,8 +1064,8 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
                      uint32_t ldy, int32_t* err, void* stream)
 {
     const bool pair = (X == nullptr);
-    if (!edge_mlp_args_ok(K1, X, ldx, recv, send, H, ldh, Ef, W1, b1, W2, b2,
-                          W3, b3, err) ||
+    if (!edge_mlp_args_ok(K1, true, X, ldx, recv, send, H, ldh, Ef, W1, b1, W2,
+                          b2, W3, b3, err) ||
         !Y || ldy < 64 || ldy % 8 || !a16(Y))
         return AQUA_ERR_INVALID;
     if (E == 0)
@@ -1078,6 +1084,14 @@ aqua_gnn_edge_mlp_tc(uint32_t E, uint32_t K1, const uint16_t* X, uint32_t ldx,
             <<<grid, kEdgeThreads, edge_mlp_smem<144>(), s>>>(
                 E, nullptr, 0, recv, send, H, ldh, Ef, W1, b1, W2, b2, W3, b3,
                 act1, act2, act3, Y, ldy, err, (uint32_t)aqua::g_debug_fake_timeout, 0u, nullptr, 0.f, 0u);
+    } else if (K1 == 80) {
+        // the first node MLP, n1 (80-wide rows): 70 KB, three CTAs per SM
+        const uint32_t cap = (uint32_t)sms * edge_ctas_per_sm<false>();
+        const uint32_t grid = tiles < cap ? tiles : cap;
+        k_edge_mlp_tc<80, false, false>
+            <<<grid, kEdgeThreads, edge_mlp_smem<80>(), s>>>(
+                E, X, ldx, nullptr, nullptr, nullptr, 0, nullptr, W1, b1, W2,
+                b2, W3, b3, act1, act2, act3, Y, ldy, err, (uint32_t)aqua::g_debug_fake_timeout, 0u, nullptr, 0.f, 0u);
     } else {
         // 52 KB: three CTAs per SM (registers; 192 TMEM columns)
         const uint32_t cap = (uint32_t)sms * edge_ctas_per_sm<false>();
@@ -1103,7 +1117,7 @@ aqua_gnn_edge_mlp_sum_tc(uint32_t n_nodes, uint32_t E, uint32_t K1,
                          int32_t* err, void* stream)
 {
     const bool pair = (X == nullptr);
-    if (!edge_mlp_args_ok(K1, X, ldx, recv, send, H, ldh, Ef, W1, b1, W2, b2,
+    if (!edge_mlp_args_ok(K1, false, X, ldx, recv, send, H, ldh, Ef, W1, b1, W2, b2,
                           W3, b3, err) ||
         !offsets || !recv || !out || !a16(out) || ld % 8 || col % 8 ||
         col + 64 > ld || E >= 0x80000000u)

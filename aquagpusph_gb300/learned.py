@@ -431,12 +431,15 @@ class Network:
                     self._lin(name, cur, ldc, M, _vp(0), 0, out, ldo)
         return A, Z
 
-    def _edge_mlp_fused(self, prefix, E, X=None, ldx=0, H=None, ldh=0, Ef=None):
+    def _edge_mlp_fused(self, prefix, E, X=None, ldx=0, H=None, ldh=0, Ef=None,
+                        out=None, ldo=64):
         """The three layers of an edge MLP in one tcgen05 kernel (inference:
-        no activations kept); returns the E x 64 bf16 output."""
+        no activations kept); returns the E x 64 bf16 output, or writes it
+        to ``out`` (rows ``ldo`` apart) if given.  The first node MLP (n1,
+        80-wide rows) runs through the same kernel."""
         torch = _torch()
         m = self.model
-        y = self._buf((max(E, 1), 64), torch.bfloat16)
+        y = self._buf((max(E, 1), 64), torch.bfloat16) if out is None else None
         names = [f"{prefix}_{k}" for k in range(3)]
         acts = [m.offs[nm][4] for nm in names]
         k1 = m.offs[names[0]][3]
@@ -448,7 +451,8 @@ class Network:
             H or _vp(0), ldh, Ef or _vp(0),
             m.W(names[0]), m.b(names[0]), m.W(names[1]), m.b(names[1]),
             m.W(names[2]), m.b(names[2]), acts[0], acts[1], acts[2],
-            _p(y), 64, _p(self.err), self.s))
+            _p(y) if out is None else out, 64 if out is None else ldo,
+            _p(self.err), self.s))
         return y
 
     def _edge_mlp_sum(self, prefix, out, ld, X=None, ldx=0, H=None, ldh=0,
@@ -511,8 +515,12 @@ class Network:
         c["n1_in"] = n1_in
         n2_in = self._buf((n, 144), torch.bfloat16)
         H = _vp(n2_in.data_ptr() + 2 * 64)
-        A, Z = self._mlp("n1", _p(n1_in), 80, n, train, out=H, ldo=144)
-        c["n1"] = (A, Z)
+        if fused:
+            self._edge_mlp_fused("n1", n, X=_p(n1_in), ldx=80, out=H, ldo=144)
+            c["n1"] = ([], [])
+        else:
+            A, Z = self._mlp("n1", _p(n1_in), 80, n, train, out=H, ldo=144)
+            c["n1"] = (A, Z)
         if summed:
             self._edge_mlp_sum("e2", n2_in, 144, H=H, ldh=144, Ef=_p(E0))
         else:

@@ -141,8 +141,9 @@ aqua_status aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N,
 /* A whole three-layer edge MLP on the tensor cores, activations on chip:
  * Y = L3(act3)(L2(act2)(L1(act1)(X))), 64-wide layers (W1: 64 x K1, W2, W3:
  * 64 x 64, bf16; biases f32), Y: E x 64 bf16 at ldy.  The layer-1 input is
- * the rows of X (K1 = AQUA_GNN_FEATURES, ldx) or, with X = NULL, the
- * concatenation [H[recv[e]], H[send[e]], Ef[e]] (K1 = 144) that
+ * the rows of X (ldx; K1 = AQUA_GNN_FEATURES, or 80 for the first node
+ * MLP) or, with X = NULL, the concatenation [H[recv[e]], H[send[e]], Ef[e]]
+ * (K1 = 144) that
  * aqua_gnn_gather_pair builds -- gathered on chip instead.  Bit-identical to
  * three aqua_gnn_linear_fwd_tc calls with the intermediate activations
  * rounded to bf16.  A time-out of the bounded waits sets *err. */

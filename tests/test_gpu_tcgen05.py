@@ -79,26 +79,34 @@ def weights(torch, rng, K1):
     return Ws, bs
 
 
+@pytest.mark.parametrize("K1", [16, 80])
 @pytest.mark.parametrize("E", [1, 127, 128, 1000, 100000])
-def test_fused_edge_mlp_rows_equals_three_layers(torch, E):
-    """Layer-1 input from rows (the first round's edge features)."""
+def test_fused_edge_mlp_rows_equals_three_layers(torch, E, K1):
+    """Layer-1 input from rows: the first message-passing step's edge
+    features (16 wide), or the first node MLP's input (80 wide, output
+    written to columns 64..127 of rows 144 apart)."""
     from aquagpusph_gb300 import learned as Lm
     L = Lm.lib()
-    rng = np.random.default_rng(E)
-    X = torch.from_numpy(G.bf16(rng.normal(0, 1, (E, 16)).astype(np.float32))
+    rng = np.random.default_rng(E + K1)
+    X = torch.from_numpy(G.bf16(rng.normal(0, 1, (E, K1)).astype(np.float32))
                          ).cuda().to(torch.bfloat16)
-    Ws, bs = weights(torch, rng, 16)
+    Ws, bs = weights(torch, rng, K1)
     acts = (1, 1, 0)
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
-    ref = three_layers(torch, Lm, L, X, 16, Ws, bs, acts, err)
-    Y = torch.empty((E, 64), dtype=torch.bfloat16, device="cuda")
-    assert L.aqua_gnn_edge_mlp_tc(E, 16, Lm._p(X), 16, None, None, None, 0, None,
+    ref = three_layers(torch, Lm, L, X, K1, Ws, bs, acts, err)
+    ld = 64 if K1 == 16 else 144
+    Yb = torch.full((E, ld), -1, dtype=torch.int16, device="cuda")
+    col = 0 if K1 == 16 else 64
+    assert L.aqua_gnn_edge_mlp_tc(E, K1, Lm._p(X), K1, None, None, None, 0, None,
                                   Lm._p(Ws[0]), Lm._p(bs[0]), Lm._p(Ws[1]),
                                   Lm._p(bs[1]), Lm._p(Ws[2]), Lm._p(bs[2]),
-                                  *acts, Lm._p(Y), 64, Lm._p(err), None) == 0
+                                  *acts, Lm._vp(Yb.data_ptr() + 2 * col), ld,
+                                  Lm._p(err), None) == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 0
-    assert torch.equal(Y.view(torch.int16), ref.view(torch.int16))
+    assert torch.equal(Yb[:, col:col + 64], ref.view(torch.int16))
+    # the other columns of the rows are not written
+    assert bool((Yb[:, :col] == -1).all()) and bool((Yb[:, col + 64:] == -1).all())
 
 
 @pytest.mark.parametrize("E,n", [(1, 3), (300, 40), (100000, 2500),
