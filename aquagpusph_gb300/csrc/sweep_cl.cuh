@@ -57,10 +57,9 @@ namespace {
 constexpr int kClListCap = 192;      // fluid survivors per warp (128 per round
                                      // of the mask scan, drained above 64)
 constexpr int kClWallCap = 192;      // boundary-element survivors per warp
-// per staged record: bit o (o < 8) = within the support of the cell's
-// octant box o; the record's kind
-constexpr uint32_t kMaskFluid = 1u << 8;
-constexpr uint32_t kMaskWall = 1u << 9;
+// per staged record: bit o (o < 8) of a fluid record, bit 8 + o of a
+// boundary element = within the support of the cell's octant box o
+constexpr uint32_t kMaskWallShift = 8;
 constexpr int kClMaxPieces = 32;     // staged runs per pass
 constexpr uint32_t kClWaitLimit = 1u << 22;
 
@@ -74,7 +73,7 @@ struct ClSmem
     uint16_t list[NW][kClListCap + 4];   // + room for the padding quad
     uint16_t wall[NW][kClWallCap + 4];
     // the staged boundary elements, by warp-sized chunks of the staging
-    alignas(8) uint16_t mask[CAP + 4];  // per staged record (kMaskFluid, kMaskWall, octants)
+    alignas(8) uint16_t mask[CAP + 4];  // per staged record: octants by kind
     float ivl[12];               // octant boxes: axis a, half h: [lo, hi] at 4 a + 2 h
     uint4 piece[kClMaxPieces];   // (slot, sorted first, count, -)
     uint2 row[9];                // (sorted first, count) of each row
@@ -626,8 +625,8 @@ k_sweep_cl(Consts c, StepArgs a)
             }
             for (uint32_t k = tid; k < nst; k += NW * 32) {
                 const float4 pc = S.r0[k];
-                uint32_t m = pc.w > 0.f ? kMaskFluid : (pc.w < 0.f ? kMaskWall : 0u);
-                if (m) {
+                uint32_t m = 0u;
+                if (pc.w != 0.f) {
                     const float x[3] = { pc.x, pc.y, pc.z };
                     float d2[6];
 #pragma unroll
@@ -642,6 +641,8 @@ k_sweep_cl(Consts c, StepArgs a)
                     for (int o = 0; o < 8; o++)
                         if (dxy[o & 3] + d2[4 + (o >> 2)] < R2)
                             m |= 1u << o;
+                    if (pc.w < 0.f)
+                        m <<= kMaskWallShift;
                 }
                 S.mask[k] = (uint16_t)m;
             }
@@ -801,14 +802,17 @@ k_sweep_cl(Consts c, StepArgs a)
                 auto fluid_pair = [&](const float4 pj, const float4 vj) {
                     const float d0 = pj.x - r0i.x, d1 = pj.y - r0i.y, d2 = pj.z - r0i.z;
                     const float rr = d0 * d0 + d1 * d1 + d2 * d2;
-                    const float qq = sqrtf(rr) * c.inv_H;
-                    // (2 - q)^+: zero at and beyond the support (2)
-                    const float tq = fmaxf(2.f - qq, 0.f);
+                    const float rd = sqrtf(rr);
+                    // (2 - q)^+ with q = rd / H: zero at and beyond the
+                    // support (2)
+                    const float tq = fmaxf(fmaf(-rd, c.inv_H, 2.f), 0.f);
                     const float tq2 = tq * tq;
-                    // pj.w = CONW W-factor * m/rho: W(q) CONW m/rho, and
-                    // F(q) CONF m/rho up to the factor f_over_w
-                    shep = shep + (1.f + 2.f * qq) * tq2 * tq2 * pj.w;
+                    // pj.w = CONW W-factor * m/rho: F(q) CONF m/rho up to
+                    // the factor f_over_w, and W(q) CONW m/rho =
+                    // (1 + 2q) (2 - q) gf, summed here as half of it
+                    // ((1/2 + q) (2 - q) gf; doubled once after the sums)
                     const float gf = tq2 * tq * pj.w;
+                    shep = fmaf(fmaf(rd, c.inv_H, 0.5f) * tq, gf, shep);
                     const float dv0 = vj.x - r1i.x, dv1 = vj.y - r1i.y, dv2 = vj.z - r1i.z;
                     const float udr = dv0 * d0 + dv1 * d1 + dv2 * d2;
                     const float t = (pi + vj.w) * gf;
@@ -898,7 +902,7 @@ k_sweep_cl(Consts c, StepArgs a)
                             if (q != 0)
                                 o[k] = 0.f;
                         }
-                        shep += o[0];
+                        shep += 0.5f * o[0];  // doubled with the pair sums
                         gp0 += o[1];
                         gp1 += o[2];
                         gp2 += o[3];
@@ -908,7 +912,8 @@ k_sweep_cl(Consts c, StepArgs a)
                     }
                     uint32_t fill = 0;
                     uint32_t wdone = wfill;  // wall entries already summed
-                    const uint32_t wkind = any_fluid ? kMaskWall : 0u;
+                    // the boundary elements matter to fluid particles only
+                    const uint32_t wmask = any_fluid ? omask << kMaskWallShift : 0u;
                     // 128 records per round, four per lane (records 4l ..
                     // 4l+3), listed in staging order
                     for (uint32_t base = 0; base < nst; base += 128) {
@@ -918,19 +923,17 @@ k_sweep_cl(Consts c, StepArgs a)
                             mm = *reinterpret_cast<const uint2*>(&S.mask[k0]);
                         const uint32_t m[4] = { mm.x & 0xffffu, mm.x >> 16, mm.y & 0xffffu, mm.y >> 16 };
                         bool fl[4], wa[4];
-                        unsigned bf[4], bw[4];
+                        unsigned bw[4];
                         uint32_t before = 0, wbefore = 0, tot = 0, wtot = 0;
 #pragma unroll
                         for (int u = 0; u < 4; u++) {
-                            const bool nu = (m[u] & omask) != 0u;
-                            fl[u] = nu && (m[u] & kMaskFluid);
-                            wa[u] = nu && (m[u] & wkind);
-                            bf[u] = __ballot_sync(0xffffffffu, fl[u]);
+                            fl[u] = (m[u] & omask) != 0u;
+                            wa[u] = (m[u] & wmask) != 0u;
+                            const unsigned bf = __ballot_sync(0xffffffffu, fl[u]);
                             bw[u] = __ballot_sync(0xffffffffu, wa[u]);
-                            before += (uint32_t)__popc(bf[u] & lt);
-                            wbefore += (uint32_t)__popc(bw[u] & lt);
-                            tot += (uint32_t)__popc(bf[u]);
-                            wtot += (uint32_t)__popc(bw[u]);
+                            before += (uint32_t)__popc(bf & lt);
+                            tot += (uint32_t)__popc(bf);
+                            wtot |= bw[u];
                         }
                         {
                             uint32_t p = fill + before;
@@ -941,6 +944,13 @@ k_sweep_cl(Consts c, StepArgs a)
                         }
                         fill += tot;
                         if (wtot) {
+#pragma unroll
+                            for (int u = 0; u < 4; u++)
+                                wbefore += (uint32_t)__popc(bw[u] & lt);
+                            wtot = 0;
+#pragma unroll
+                            for (int u = 0; u < 4; u++)
+                                wtot += (uint32_t)__popc(bw[u]);
                             if (wfill + wtot > (uint32_t)kClWallCap) {
                                 // the wall list is full: sum it, and let the
                                 // epilogue walk the walls from global memory
@@ -994,6 +1004,7 @@ k_sweep_cl(Consts c, StepArgs a)
                 if (failed)
                     break;
                 if (have) {
+                    shep = shep + shep;  // the pair sums hold half of it
                     // ---- the four partial sums of each particle
                     float* acc[13] = { &shep, &gp0, &gp1, &gp2, &lu0, &lu1, &lu2,
                                        &du, &lp, &gw0, &gw1, &gw2, &dbi };
