@@ -809,10 +809,12 @@ k_sweep_cl(Consts c, StepArgs a)
                     const float tq2 = tq * tq;
                     // pj.w = CONW W-factor * m/rho: F(q) CONF m/rho up to
                     // the factor f_over_w, and W(q) CONW m/rho =
-                    // (1 + 2q) (2 - q) gf, summed here as half of it
-                    // ((1/2 + q) (2 - q) gf; doubled once after the sums)
+                    // (1 + 2q) (2 - q) gf, summed here as half of it,
+                    // (1/2 + q) (2 - q) gf = (5/2 (2 - q) - (2 - q)^2) gf
+                    // (zero with gf beyond the support; doubled once after
+                    // the sums)
                     const float gf = tq2 * tq * pj.w;
-                    shep = fmaf(fmaf(rd, c.inv_H, 0.5f) * tq, gf, shep);
+                    shep = fmaf(fmaf(2.5f, tq, -tq2), gf, shep);
                     const float dv0 = vj.x - r1i.x, dv1 = vj.y - r1i.y, dv2 = vj.z - r1i.z;
                     const float udr = dv0 * d0 + dv1 * d1 + dv2 * d2;
                     const float t = (pi + vj.w) * gf;

@@ -225,9 +225,9 @@ SWEEP_DRAM_BYTES_PER_PARTICLE = {"k_sweep_cl<3>": 168.5, "k_sweep<3>": 170.5}
 # FP32 instructions of one fluid-fluid pair of the fast sweep, counted from
 # the source of the clustered sweep's pair (separation 3, |r|^2 3, sqrt 1,
 # (2-q)^+ 2 with q folded into a fused multiply-add, (2-q)^2 1, F factor 2,
-# Shepard term 3, velocity difference 3, (u_ij . r_ij) 3, pressure factor
+# Shepard term 2, velocity difference 3, (u_ij . r_ij) 3, pressure factor
 # 2, grad p 3, lap u 3, div u 1, lap p 2), a fused multiply-add counted once
-PAIR_FP32_INSTR = 32
+PAIR_FP32_INSTR = 31
 # FP32 lanes x SMs of one GB300 (the instruction rate of the FMA pipes at
 # the SM clock)
 FP32_LANES = 128 * 152
