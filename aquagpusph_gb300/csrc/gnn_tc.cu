@@ -57,15 +57,20 @@ make_idesc(uint32_t n)
            ((uint32_t)(kTcRows >> 4) << 24);
 }
 
-// SiLU as z * sigmoid(z) with sigmoid(z) = (1 + tanh(z / 2)) / 2 on the
-// hardware tanh (tanh.approx.f32, about 2^-11 relative error): well below
-// the bf16 rounding of the activation that follows
-__device__ __forceinline__ float
-silu_f(float z)
+// SiLU of two bf16 values (a packed pair) in packed bf16 arithmetic:
+// z * sigmoid(z), sigmoid(z) = (1 + tanh(z / 2)) / 2 on the hardware tanh
+// (tanh.approx.bf16x2); four instructions for the pair, each result
+// rounded to bf16
+__device__ __forceinline__ uint32_t
+silu_bf16x2(uint32_t z)
 {
-    float t;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
-    return z * fmaf(0.5f, t, 0.5f);
+    const uint32_t half = 0x3f003f00u;  // 0.5 in both halves
+    uint32_t h, t, s, y;
+    asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(z), "r"(half));
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
+    asm("fma.rn.bf16x2 %0, %1, %2, %2;" : "=r"(s) : "r"(t), "r"(half));
+    asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(y) : "r"(z), "r"(s));
+    return y;
 }
 
 // two floats rounded to bf16 (round to nearest even), lo in the low half
@@ -193,9 +198,9 @@ k_linear_fwd_tc(uint32_t M, uint32_t K, const uint16_t* __restrict__ X,
                 if (Y) {
                     uint32_t p[8];
                     for (int j = 0; j < 8; j++) {
-                        const float a0 = act == AQUA_ACT_SILU ? silu_f(z[2 * j]) : z[2 * j];
-                        const float a1 = act == AQUA_ACT_SILU ? silu_f(z[2 * j + 1]) : z[2 * j + 1];
-                        p[j] = pack2(a0, a1);
+                        p[j] = pack2(z[2 * j], z[2 * j + 1]);
+                        if (act == AQUA_ACT_SILU)
+                            p[j] = silu_bf16x2(p[j]);
                     }
                     uint4* dst = reinterpret_cast<uint4*>(Y + (size_t)row * ldy + c0);
                     dst[0] = make_uint4(p[0], p[1], p[2], p[3]);
@@ -423,13 +428,11 @@ k_edge_mlp_tc(uint32_t E, const uint16_t* __restrict__ X, uint32_t ldx,
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const int c = q * 8 + 2 * j;
-                float z0 = __uint_as_float(v[c]) + bias[c];
-                float z1 = __uint_as_float(v[c + 1]) + bias[c + 1];
-                if (act == AQUA_ACT_SILU) {
-                    z0 = silu_f(z0);
-                    z1 = silu_f(z1);
-                }
+                const float z0 = __uint_as_float(v[c]) + bias[c];
+                const float z1 = __uint_as_float(v[c + 1]) + bias[c + 1];
                 p[j] = pack2(z0, z1);
+                if (act == AQUA_ACT_SILU)
+                    p[j] = silu_bf16x2(p[j]);
             }
             emit((int)(half * 4u) + q, make_uint4(p[0], p[1], p[2], p[3]));
         }
