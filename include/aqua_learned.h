@@ -131,8 +131,11 @@ aqua_status aqua_gnn_linear_fwd(uint32_t M, uint32_t K, uint32_t N,
                                 int32_t act, void* stream);
 /* The same forward on the 5th-generation tensor cores (tcgen05.mma with a
  * tensor-memory accumulator, 128-row tiles), for N = 64: all pointers
- * 16-byte aligned, ldz % 4 == 0.  A time-out of its bounded waits sets
- * *err (device int, set to 0 by the caller) instead of hanging. */
+ * 16-byte aligned, ldz % 4 == 0.  Z is the FP32 accumulator plus bias; Y
+ * is Z rounded to bf16 and, for SiLU, activated in packed bf16 arithmetic
+ * (within a few bf16 roundings of aqua_gnn_linear_fwd's FP32 SiLU).  A
+ * time-out of its bounded waits sets *err (device int, set to 0 by the
+ * caller) instead of hanging. */
 aqua_status aqua_gnn_linear_fwd_tc(uint32_t M, uint32_t K, uint32_t N,
                                    const uint16_t* X, uint32_t ldx,
                                    const uint16_t* W, const float* b, float* Z,
