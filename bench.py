@@ -218,9 +218,9 @@ def job_throughput(world: int, n_per_rank: int, steps: int, seconds: float) -> f
 
 # DRAM bytes per particle of the fused sweep from one ncu capture of the
 # 1.89M-particle profiling case (dram__bytes_read.sum + dram__bytes_write.sum
-# over N; profiles/k_sweep_cl_c1m.md, profiles/k_sweep_c1m.md), scaled to a
-# launch by N.
-SWEEP_DRAM_BYTES_PER_PARTICLE = {"k_sweep_cl<3>": 168.5, "k_sweep<3>": 170.5}
+# over N: 273.3 + 90.3 MB for the clustered sweep, the particle records plus
+# its cluster tables), scaled to a launch by N.
+SWEEP_DRAM_BYTES_PER_PARTICLE = {"k_sweep_cl<3>": 192.1, "k_sweep<3>": 170.5}
 
 # FP32 instructions of one fluid-fluid pair of the fast sweep, counted from
 # the source of the clustered sweep's pair (separation 3, |r|^2 3, sqrt 1,
