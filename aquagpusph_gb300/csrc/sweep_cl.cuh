@@ -20,11 +20,11 @@
 // read the same record (a broadcast, free of bank conflicts).
 // The list holds the staged candidates within the support of the octant
 // boxes of the cluster's particles.  After each staging the block
-// classifies every staged record once: its kind (fluid, boundary element)
-// and the octant boxes of the cell it comes within the support of (a box
-// per octant, spanning, per axis and half, the cell's particles there).
-// Each cluster then scans those 16-bit masks and compacts its candidates
-// with ballots.  About 60% of the evaluated pairs lie in the support on a
+// classifies every staged record once into a 16-bit mask: the octant boxes
+// of the cell it comes within the support of (a box per octant, spanning,
+// per axis and half, the cell's particles there), in the low byte for a
+// fluid record and the high byte for a boundary element.  Each cluster then
+// scans those masks and compacts its candidates with ballots.  About 60% of the evaluated pairs lie in the support on a
 // lattice, against about a third of the lanes in k_sweep.  Pairs outside
 // the support add exact zeros (the kernel factor is cut to zero at
 // q >= SUPPORT), so the lists only have to be conservative: each octant
